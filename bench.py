@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Origami GB300 mergesort benchmark.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl origami|reference]
+
+Workload: full ascending sort of 268,435,456 uint32 keys (1 GiB) drawn
+uniformly from [0, 2^32), one array per GPU (replicas: no data exchange
+between GPUs, so "scaling" is weak). A step is one sort of that array.
+
+  value   Gkeys/s with the keys already resident in HBM; each step's input is
+          restored from a pristine device copy outside the step's CUDA events
+          (the 1 GiB input is larger than L2, so no extra flush is needed).
+  e2e     the same metric through the C ABI with pinned HOST buffers: the
+          host->device copy, the sort and the device->host copy are all timed.
+  roofline  the dominant kernel's algorithmic bytes per launch (read + write of
+          every item once) over its average CUDA-event launch time, against the
+          measured HBM copy bandwidth in MEASURED_PEAKS.json.
+  cpu_baseline  the oracle (C restatement of the reference pipeline, all host
+          threads) on the same workload, timed on this machine's host cores.
+
+`--impl reference` times the reference's CPU sort instead (the compiled
+reference when it loads on this host, otherwise the oracle port) and prints the
+same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "origami-sort_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+N_KEYS = 1 << 28
+METRIC = "Gkeys/s sorting 1 GB uint32 on 1 GB300 (% HBM roofline); batched p50/p99 latency"
+WORKLOAD = "full sort of 268,435,456 uint32 keys (1 GiB), uniform over [0, 2^32)"
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index, interval_ms=50):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.gpu = gpu_index
+        self.proc = None
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", f"-lms={interval_ms}"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
+        time.sleep(0.12)
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(n_full, seconds=12.0):
+    """Oracle (C restatement of the reference pipeline) with every host thread, on
+    a bounded sample of the workload: the largest power-of-two prefix that sorts
+    in a few seconds, repeated until ~`seconds` of CPU work."""
+    import numpy as np
+
+    import oracle as orc
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(2026)
+    n = min(n_full, 1 << 26)
+    src = rng.integers(0, 1 << 32, n, dtype=np.uint32)
+    d = orc.empty(orc.U32, n)
+    o = orc.empty(orc.U32, n)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(times) < 2:
+        d[:] = src
+        t0 = time.perf_counter()
+        r = orc.sort_multi_thread_inplace(orc.U32, d, o, threads, 16)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 20:
+            break
+    assert orc.is_sorted(orc.U32, r)
+    best = min(times)
+    return {"value": n / best / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+            "sample": f"{n} uniform uint32 keys (1/{n_full // n} of the workload), "
+                      f"oracle sort_multi_thread restatement, min_k=16, best of {len(times)} runs"}
+
+
+def run_reference(args):
+    """CPU reference arm: the reference's own multithreaded sort when it loads on
+    this host (x86 builds from oracle/_ref), else the oracle port of it."""
+    import numpy as np
+
+    import oracle as orc
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    kind_label = "port"
+    ref = None
+    if "a2_u32" in orc.ref_variants():
+        try:
+            ref = orc.ref_lib("a2_u32")
+            kind_label = "reference"
+        except OSError:
+            ref = None
+    orc.build()
+    n = N_KEYS
+    rng = np.random.default_rng(7)
+    src = rng.integers(0, 1 << 32, n, dtype=np.uint32)
+    d = orc.empty(orc.U32, n)
+    o = orc.empty(orc.U32, n)
+    kbuf = orc.empty(orc.U32, (threads * 8 << 20) // 4 + (1 << 20)) if ref is not None else None
+
+    def one():
+        d[:] = src
+        t0 = time.perf_counter()
+        if ref is not None:
+            ref.ref_sort_multi_thread(d.ctypes.data, o.ctypes.data, n, threads, threads, 16,
+                                      kbuf.ctypes.data)
+        else:
+            orc.sort_multi_thread_inplace(orc.U32, d, o, threads, 16)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one()
+    times = [one() for _ in range(args.steps)]
+    total = sum(times)
+    value = n * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic: uniform uint32, numpy seed 7",
+        "config": {"workload": WORKLOAD, "n": n, "threads": threads, "min_k": 16},
+        "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": threads, "kind": kind_label,
+                         "sample": f"the whole {n}-key workload per step"},
+        "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="origami", choices=["origami", "reference"])
+    ap.add_argument("--n", type=int, default=N_KEYS)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    import origami_gpu as og
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    og.lib()
+    n = args.n
+    kind = og.U32
+    dev = torch.device("cuda", local)
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    pristine = torch.randint(-(2**31), 2**31, (n,), dtype=torch.int32, device=dev, generator=g)
+    d = torch.empty_like(pristine)
+    tmp = torch.empty_like(pristine)
+
+    def step():
+        d.copy_(pristine)
+        return og.sort(d, tmp, kind=kind)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # correctness of the measured configuration (outside the timed region)
+    out = step()
+    torch.cuda.synchronize()
+    k = out.to(torch.int64) & 0xFFFFFFFF
+    ok = bool((k[1:] >= k[:-1]).all().item()) and int(k.sum().item()) == int(
+        (pristine.to(torch.int64) & 0xFFFFFFFF).sum().item())
+    del k
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    og.profile_enable(True)
+    launches0 = og.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        d.copy_(pristine)
+        starts[i].record()
+        og.sort(d, tmp, kind=kind)
+        ends[i].record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = og.launch_count() - launches0
+    report = og.profile_report()
+    og.profile_enable(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms / 1e3) / 1e9
+    peak, peak_src = peaks()
+    item = 4
+    # dominant kernel and its roofline
+    dom = max(report.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    per_launch_ms = dom_ms / dom_launches
+    bytes_per_launch = 2 * n * item
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    passes = sum(c for name, (c, _) in report.items()
+                 if name.startswith(("block_sort", "pair_merge", "kway_merge"))) // args.steps
+    ms_step = total_ms / args.steps
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get(dom_name.split("<")[0])
+
+    e2e = None
+    if args.e2e_steps > 0:
+        h_src = pristine.cpu().numpy().view("uint32")
+        h_d = og.empty_host("u32", n, pinned=True)
+        h_t = og.empty_host("u32", n, pinned=True)
+        ts = []
+        for i in range(args.e2e_steps + 1):
+            h_d[:] = h_src
+            t0 = time.perf_counter()
+            r = og.sort(h_d, h_t)
+            t1 = time.perf_counter()
+            if i > 0:
+                ts.append(t1 - t0)
+        import numpy as np
+        e2e_ok = bool(np.all(r[1:] >= r[:-1]))
+        e2e = {"value": n / statistics.mean(ts) / 1e9, "unit": "Gkeys/s",
+               "h2d_bytes_per_step": n * item, "d2h_bytes_per_step": n * item,
+               "ms_per_step": 1e3 * statistics.mean(ts), "steps": len(ts), "correct": e2e_ok}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(n)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic: uniform uint32 keys from torch.randint on the device (seed 1234+rank)",
+        "config": {"workload": WORKLOAD, "n": n, "item_bytes": item,
+                   "l2": "input (1 GiB) larger than L2; restored from a pristine copy before each step",
+                   "hbm_passes": passes, "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                     "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+                     "traffic": traffic,
+                     "pipeline_frac": (2 * n * item * passes / (ms_step / 1e3) / 1e9) / peak},
+        "kernels": {k: {"launches": c, "ms": ms} for k, (c, ms) in report.items()},
+        "gpu_launches": launches,
+        "correct": ok,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,161 @@
+/*
+ * origami_gpu.h - C ABI of the GB300 (sm_103a) Origami mergesort.
+ *
+ * Drop-in for the CPU sort entry points of arif-arman/origami-sort. Every call
+ * takes plain pointers and sizes; nothing here needs CUDA or torch headers
+ * (streams are passed as `void*`, meaning a cudaStream_t; NULL = the legacy
+ * default stream).
+ *
+ * Item kinds:
+ *   u32   uint32_t keys                                    (reference `ui`, KEY_TYPE 0)
+ *   u64   uint64_t keys, unsigned order                    (superset of the reference)
+ *   i64   int64_t keys, signed order                       (reference `i64`, KEY_TYPE 1)
+ *   kv64  {int64_t key; int64_t value;}, 16 B, by key      (reference KeyValue<i64,i64>, KEY_TYPE 2)
+ *   kvu64 {uint64_t key; uint64_t value;}, 16 B, by key    (superset of the reference)
+ * Key-value sorts are stable: equal keys keep their input order.
+ *
+ * Result-buffer convention (reference sorter.h:3852,3914): the sorted output
+ * lands in one of the two caller buffers and *result says which. By default it
+ * is `d`; ORIGAMI_FLAG_RESULT_IN_TMP asks for `tmp`.
+ *
+ * Return value: ORIGAMI_OK (0) or a negative ORIGAMI_ERR_* code; the message is
+ * kept per thread and returned by origami_last_error(). No call ever exits the
+ * process (the reference does: commons.h:103-104).
+ */
+#ifndef ORIGAMI_GPU_H
+#define ORIGAMI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORIGAMI_GPU_VERSION 100
+
+/* status codes */
+#define ORIGAMI_OK 0
+#define ORIGAMI_ERR_INVALID (-1)   /* null pointer, bad size, bad sort_n, overlapping buffers */
+#define ORIGAMI_ERR_ALIGN (-2)     /* pointer not aligned to the item size */
+#define ORIGAMI_ERR_OOM (-3)       /* device memory exhausted / over the arena budget */
+#define ORIGAMI_ERR_CUDA (-4)      /* a CUDA runtime call failed */
+#define ORIGAMI_ERR_TIMEOUT (-5)   /* a bounded device wait gave up */
+#define ORIGAMI_ERR_DTYPE (-6)     /* unknown item kind */
+#define ORIGAMI_ERR_NO_DEVICE (-7) /* no usable CUDA device */
+#define ORIGAMI_ERR_BUSY (-8)      /* queue full / admission refused */
+#define ORIGAMI_ERR_CANCELLED (-9) /* request cancelled before it ran */
+
+/* item kinds (same numbering as the oracle) */
+#define ORIGAMI_U32 0
+#define ORIGAMI_U64 1
+#define ORIGAMI_I64 2
+#define ORIGAMI_KV64 3
+#define ORIGAMI_KVU64 4
+
+/* flags */
+#define ORIGAMI_FLAG_RESULT_IN_TMP 0x1 /* leave the sorted output in tmp instead of d */
+#define ORIGAMI_FLAG_SYNC 0x2          /* _device calls: synchronize the stream before returning */
+
+int origami_version(void);
+const char* origami_last_error(void);
+unsigned origami_item_bytes(int kind);
+
+/*
+ * Plain sort: the drop-in for origami_sorter::sort_single_thread
+ * (reference sorter.h:3851-3915) and sort_multi_thread (sorter.h:4194-4287).
+ *
+ *   d, tmp   two buffers of n items each. Host pointers (pageable or pinned) are
+ *            staged through the library's device arena and the result is copied
+ *            back; device pointers are sorted in place with no copies.
+ *            tmp may be NULL: device scratch is then taken from the arena.
+ *   n        item count (any n >= 0)
+ *   sort_n   chunk size: the array is sorted in independent chunks of sort_n
+ *            items (the reference's "sort_n" / chunked sort,
+ *            bench_sort_phases.cpp:1307-1425). 0 or >= n means one full sort.
+ *            Otherwise it must be a power of two.
+ *   min_k    merge fan-in of each HBM pass (the reference's min_k, sorter.h:3875):
+ *            2 = binary merge passes, 4/8/16 = k-way passes. 0 picks the tuned value.
+ *   result   receives d or tmp.
+ * The call returns after the result is in place (host) or is enqueued on the
+ * default stream (device pointers; add ORIGAMI_FLAG_SYNC to wait).
+ */
+int origami_sort_u32(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
+                     void** result);
+int origami_sort_u64(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
+                     void** result);
+int origami_sort_i64(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
+                     void** result);
+int origami_sort_kv64(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
+                      void** result);
+int origami_sort_kvu64(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
+                       void** result);
+
+/* Device-pointer form on an explicit stream: zero-copy, asynchronous. */
+int origami_sort_u32_device(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                            int flags, void** result, void* stream);
+int origami_sort_u64_device(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                            int flags, void** result, void* stream);
+int origami_sort_i64_device(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                            int flags, void** result, void* stream);
+int origami_sort_kv64_device(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                             int flags, void** result, void* stream);
+int origami_sort_kvu64_device(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                              int flags, void** result, void* stream);
+
+/* Kind-generic forms of the two calls above. */
+int origami_sort(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                 int flags, void** result);
+int origami_sort_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                        int flags, void** result, void* stream);
+
+/*
+ * origami_merger::merge_series (reference merger.h:4220-4228): binary merge
+ * levels over device buffers, from sorted runs of merge_start items up to runs
+ * of sort_n items (both powers of two, merge_start < sort_n), ping-ponging
+ * src/dst. *result receives src or dst, whichever holds the output.
+ */
+int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint64_t merge_start,
+                                uint64_t sort_n, void** result, void* stream);
+
+/*
+ * MergeTree::merge(X, endX, C, n, ...) (reference merge_tree.h:2792, 3410):
+ * way-way merge of the sorted device streams [X[i], endX[i]) into C. X and endX
+ * are HOST arrays of `way` device pointers (way <= 16). Ties go to the lower
+ * stream, so the merge is stable across streams.
+ */
+int origami_merge_tree_device(int kind, void* const* X, void* const* endX, void* C, unsigned way,
+                              void* stream);
+
+/*
+ * partition_templated::Partition_Ptrs (reference Partition.h:118-166) as a
+ * merge-path splitter search: for the K sorted device streams
+ * [L[i], R[i]) and each requested output rank ranks[j] (host array, count
+ * n_ranks), writes split offsets splits[j*K + i] (host array) such that taking
+ * the first splits[j*K+i] items of every stream gives exactly the ranks[j]
+ * smallest items, ties ordered by stream. K <= 16.
+ */
+int origami_partition_device(int kind, void* const* L, void* const* R, unsigned K,
+                             const uint64_t* ranks, uint64_t n_ranks, uint64_t* splits,
+                             void* stream);
+
+/*
+ * Launch accounting and profiling. Every kernel the library launches is
+ * counted. While profiling is enabled each launch is also bracketed by two CUDA
+ * events on its own stream; origami_profile_report() waits for them and writes
+ * one "kernel,launches,total_ms" line per kernel into buf (returns the length,
+ * or a negative status). Enabling (or disabling) clears earlier records.
+ */
+int origami_profile_enable(int on);
+int origami_profile_report(char* buf, uint64_t cap);
+uint64_t origami_launch_count(void);
+
+/* Device arena used by the host-pointer calls and by the serving loop. */
+int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */
+int origami_arena_trim(void);               /* return cached memory to the driver */
+uint64_t origami_arena_bytes_in_use(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ORIGAMI_GPU_H */

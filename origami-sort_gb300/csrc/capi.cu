@@ -1,0 +1,403 @@
+// C ABI (include/origami_gpu.h): argument validation, the pooled device arena,
+// host-pointer staging and dispatch onto the typed pipelines.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/origami_gpu.h"
+#include "dispatch.h"
+#include "pipeline.cuh"
+#include "profiler.h"
+
+namespace origami {
+
+// ---- launch accounting / profiling (profiler.h) ----
+namespace {
+std::atomic<uint64_t> g_launches{0};
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+std::vector<ProfRec> g_recs;
+std::vector<cudaEvent_t> g_event_pool;
+
+cudaEvent_t take_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+bool profiling_on() { return g_prof_on.load(std::memory_order_relaxed); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int prof_begin(const char* name, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRec r{name, take_event(), take_event()};
+    cudaEventRecord(r.a, st);
+    g_recs.push_back(r);
+    return (int)g_recs.size() - 1;
+}
+
+void prof_end(int slot, cudaStream_t st) {
+    if (slot < 0) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEventRecord(g_recs[slot].b, st);
+}
+uint64_t split_slots_u32(uint64_t n);
+uint64_t split_slots_u64(uint64_t n);
+uint64_t split_slots_kv(uint64_t n);
+
+uint64_t split_slots(int kind, uint64_t n) {
+    switch (kind) {
+        case ORIGAMI_U32: return split_slots_u32(n);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return split_slots_u64(n);
+        default: return split_slots_kv(n);
+    }
+}
+}  // namespace origami
+
+using namespace origami;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ORIGAMI_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ORIGAMI_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+bool valid_kind(int kind) { return kind >= ORIGAMI_U32 && kind <= ORIGAMI_KVU64; }
+
+unsigned item_bytes(int kind) {
+    switch (kind) {
+        case ORIGAMI_U32: return 4;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return 8;
+        default: return 16;
+    }
+}
+
+uint64_t key_mask(int kind) {
+    return (kind == ORIGAMI_I64 || kind == ORIGAMI_KV64) ? 0x8000000000000000ull : 0ull;
+}
+
+// The stream-ordered allocator's default pool is the device arena: freed blocks
+// stay cached (release threshold = max) so repeated calls do not return memory
+// to the driver.
+std::once_flag g_pool_once;
+int g_pool_status = ORIGAMI_OK;
+
+int ensure_device() {
+    std::call_once(g_pool_once, [] {
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+            cudaGetLastError();
+            g_pool_status = ORIGAMI_ERR_NO_DEVICE;
+            return;
+        }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+    if (g_pool_status != ORIGAMI_OK) return fail(g_pool_status, "no CUDA device available");
+    return ORIGAMI_OK;
+}
+
+cudaStream_t worker_stream() {
+    thread_local cudaStream_t s = nullptr;
+    if (!s) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    return s;
+}
+
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int check_args(int kind, const void* d, const void* tmp, uint64_t n, uint64_t sort_n, void** result) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (!result) return fail(ORIGAMI_ERR_INVALID, "result pointer is NULL");
+    if (n > 0 && !d) return fail(ORIGAMI_ERR_INVALID, "d is NULL with n = %llu", (unsigned long long)n);
+    const unsigned s = item_bytes(kind);
+    const unsigned align = s > 8 ? 8 : s;
+    if (((uintptr_t)d % align) || (tmp && ((uintptr_t)tmp % align)))
+        return fail(ORIGAMI_ERR_ALIGN, "buffers must be %u-byte aligned", align);
+    if (n > (1ull << 40)) return fail(ORIGAMI_ERR_INVALID, "n = %llu is too large", (unsigned long long)n);
+    if (sort_n != 0 && sort_n < n && (sort_n & (sort_n - 1)) != 0)
+        return fail(ORIGAMI_ERR_INVALID, "sort_n = %llu must be 0, >= n or a power of two",
+                    (unsigned long long)sort_n);
+    if (d && tmp && n > 0) {
+        const char* a = (const char*)d;
+        const char* b = (const char*)tmp;
+        const uint64_t bytes = n * s;
+        if (a < b + bytes && b < a + bytes) return fail(ORIGAMI_ERR_INVALID, "d and tmp overlap");
+    }
+    return ORIGAMI_OK;
+}
+
+cudaError_t run_typed(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, void* want,
+                      int64_t* splits, cudaStream_t st) {
+    const uint64_t m = key_mask(kind);
+    switch (kind) {
+        case ORIGAMI_U32: return sort_u32(d, tmp, n, sort_n, m, want, splits, st, nullptr);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return sort_u64(d, tmp, n, sort_n, m, want, splits, st, nullptr);
+        default: return sort_kv(d, tmp, n, sort_n, m, want, splits, st, nullptr);
+    }
+}
+
+// Device-resident sort; the caller has validated the arguments.
+int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, int flags,
+                     void** result, cudaStream_t st) {
+    const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
+    if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
+    *result = in_tmp ? tmp : d;
+    if (n <= 1) {
+        if (n == 1 && in_tmp)
+            CK(cudaMemcpyAsync(tmp, d, item_bytes(kind), cudaMemcpyDeviceToDevice, st), "copy");
+        if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
+        return ORIGAMI_OK;
+    }
+    void* scratch = nullptr;
+    if (!tmp) CK(cudaMallocAsync(&scratch, n * item_bytes(kind), st), "scratch allocation");
+    int64_t* splits = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&splits, split_slots(kind, n) * sizeof(int64_t), st);
+    if (e != cudaSuccess) {
+        if (scratch) cudaFreeAsync(scratch, st);
+        return cuda_fail(e, "splitter allocation");
+    }
+    e = run_typed(kind, d, tmp ? tmp : scratch, n, sort_n, in_tmp ? tmp : d, splits, st);
+    cudaFreeAsync(splits, st);
+    if (scratch) cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "sort launch");
+    if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
+    return ORIGAMI_OK;
+}
+
+// Host buffers: stage through the arena, sort on the device, copy the result
+// back into d (or tmp) and return when it is there.
+int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, int flags,
+                   void** result) {
+    const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
+    if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
+    void* out = in_tmp ? tmp : d;
+    *result = out;
+    if (n == 0) return ORIGAMI_OK;
+    const uint64_t bytes = n * item_bytes(kind);
+    cudaStream_t st = worker_stream();
+    void* dd = nullptr;
+    void* dt = nullptr;
+    CK(cudaMallocAsync(&dd, bytes, st), "arena allocation");
+    cudaError_t e = cudaMallocAsync(&dt, bytes, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(dd, st);
+        return cuda_fail(e, "arena allocation");
+    }
+    int rc = ORIGAMI_OK;
+    void* dres = nullptr;
+    e = cudaMemcpyAsync(dd, d, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        rc = sort_device_impl(kind, dd, dt, n, sort_n, 0, &dres, st);
+        if (rc == ORIGAMI_OK) e = cudaMemcpyAsync(out, dres, bytes, cudaMemcpyDeviceToHost, st);
+    }
+    cudaFreeAsync(dd, st);
+    cudaFreeAsync(dt, st);
+    cudaError_t es = cudaStreamSynchronize(st);
+    if (rc != ORIGAMI_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "host staging copy");
+    if (es != cudaSuccess) return cuda_fail(es, "stream sync");
+    return ORIGAMI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int origami_version(void) { return ORIGAMI_GPU_VERSION; }
+
+const char* origami_last_error(void) { return g_last_error.c_str(); }
+
+unsigned origami_item_bytes(int kind) { return valid_kind(kind) ? item_bytes(kind) : 0; }
+
+int origami_sort_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                        int flags, void** result, void* stream) {
+    (void)min_k;
+    int rc = check_args(kind, d, tmp, n, sort_n, result);
+    if (rc != ORIGAMI_OK) return rc;
+    if ((rc = ensure_device()) != ORIGAMI_OK) return rc;
+    return sort_device_impl(kind, d, tmp, n, sort_n, flags, result, (cudaStream_t)stream);
+}
+
+int origami_sort(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                 int flags, void** result) {
+    int rc = check_args(kind, d, tmp, n, sort_n, result);
+    if (rc != ORIGAMI_OK) return rc;
+    if ((rc = ensure_device()) != ORIGAMI_OK) return rc;
+    (void)min_k;
+    if (n > 0 && is_device_pointer(d)) {
+        if (tmp && !is_device_pointer(tmp))
+            return fail(ORIGAMI_ERR_INVALID, "d is device memory but tmp is not");
+        return sort_device_impl(kind, d, tmp, n, sort_n, flags | ORIGAMI_FLAG_SYNC, result, 0);
+    }
+    return sort_host_impl(kind, d, tmp, n, sort_n, flags, result);
+}
+
+#define ORIGAMI_TYPED(name, KIND)                                                                  \
+    int origami_sort_##name(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,      \
+                            int flags, void** result) {                                            \
+        return origami_sort(KIND, d, tmp, n, sort_n, min_k, flags, result);                        \
+    }                                                                                              \
+    int origami_sort_##name##_device(void* d, void* tmp, uint64_t n, uint64_t sort_n,             \
+                                     unsigned min_k, int flags, void** result, void* stream) {     \
+        return origami_sort_device(KIND, d, tmp, n, sort_n, min_k, flags, result, stream);         \
+    }
+ORIGAMI_TYPED(u32, ORIGAMI_U32)
+ORIGAMI_TYPED(u64, ORIGAMI_U64)
+ORIGAMI_TYPED(i64, ORIGAMI_I64)
+ORIGAMI_TYPED(kv64, ORIGAMI_KV64)
+ORIGAMI_TYPED(kvu64, ORIGAMI_KVU64)
+
+int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint64_t merge_start,
+                                uint64_t sort_n, void** result, void* stream) {
+    int rc = check_args(kind, src, dst, n, sort_n, result);
+    if (rc != ORIGAMI_OK) return rc;
+    if (!dst && n > 0) return fail(ORIGAMI_ERR_INVALID, "dst is NULL");
+    if (merge_start == 0 || (merge_start & (merge_start - 1)) || sort_n == 0 ||
+        (sort_n & (sort_n - 1)) || merge_start > sort_n)
+        return fail(ORIGAMI_ERR_INVALID, "merge_start and sort_n must be powers of two, merge_start <= sort_n");
+    if ((rc = ensure_device()) != ORIGAMI_OK) return rc;
+    // merger.h:4220-4228 swaps src/dst once per level and returns src: the
+    // output is in src after an even number of levels, in dst after an odd one.
+    int levels = 0;
+    for (uint64_t r = merge_start; r < sort_n; r <<= 1) ++levels;
+    const int flags = (levels & 1) ? ORIGAMI_FLAG_RESULT_IN_TMP : 0;
+    // Merging sorted runs stably up to sort_n gives exactly the stable chunk
+    // sort of the input, which is what the pipeline computes.
+    return sort_device_impl(kind, src, dst, n, sort_n, flags, result, (cudaStream_t)stream);
+}
+
+int origami_arena_reserve(uint64_t bytes) {
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    void* p = nullptr;
+    cudaStream_t st = worker_stream();
+    CK(cudaMallocAsync(&p, bytes, st), "arena reserve");
+    CK(cudaFreeAsync(p, st), "arena reserve");
+    CK(cudaStreamSynchronize(st), "arena reserve");
+    return ORIGAMI_OK;
+}
+
+int origami_arena_trim(void) {
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    int dev = 0;
+    cudaMemPool_t pool;
+    CK(cudaGetDevice(&dev), "arena trim");
+    CK(cudaDeviceGetDefaultMemPool(&pool, dev), "arena trim");
+    CK(cudaDeviceSynchronize(), "arena trim");
+    CK(cudaMemPoolTrimTo(pool, 0), "arena trim");
+    return ORIGAMI_OK;
+}
+
+uint64_t origami_arena_bytes_in_use(void) {
+    if (ensure_device() != ORIGAMI_OK) return 0;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess)
+        return 0;
+    uint64_t v = 0;
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &v);
+    return v;
+}
+
+int origami_profile_enable(int on) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto& r : g_recs) {
+        g_event_pool.push_back(r.a);
+        g_event_pool.push_back(r.b);
+    }
+    g_recs.clear();
+    g_prof_on.store(on != 0);
+    return ORIGAMI_OK;
+}
+
+int origami_profile_report(char* buf, uint64_t cap) {
+    if (!buf || cap == 0) return fail(ORIGAMI_ERR_INVALID, "report buffer is NULL");
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::map<std::string, std::pair<uint64_t, double>> agg;
+    for (auto& r : g_recs) {
+        CK(cudaEventSynchronize(r.b), "profile sync");
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, r.a, r.b), "profile elapsed");
+        auto& e = agg[r.name];
+        e.first += 1;
+        e.second += ms;
+    }
+    std::string out;
+    char line[256];
+    for (auto& kv : agg) {
+        snprintf(line, sizeof line, "%s,%llu,%.6f\n", kv.first.c_str(),
+                 (unsigned long long)kv.second.first, kv.second.second);
+        out += line;
+    }
+    if (out.size() + 1 > cap) return fail(ORIGAMI_ERR_INVALID, "report buffer too small");
+    memcpy(buf, out.c_str(), out.size() + 1);
+    return (int)out.size();
+}
+
+uint64_t origami_launch_count(void) { return g_launches.load(); }
+
+int origami_merge_tree_device(int kind, void* const* X, void* const* endX, void* C, unsigned way,
+                              void* stream) {
+    (void)kind; (void)X; (void)endX; (void)C; (void)way; (void)stream;
+    return fail(ORIGAMI_ERR_INVALID, "merge tree entry point not built yet");
+}
+
+int origami_partition_device(int kind, void* const* L, void* const* R, unsigned K,
+                             const uint64_t* ranks, uint64_t n_ranks, uint64_t* splits,
+                             void* stream) {
+    (void)kind; (void)L; (void)R; (void)K; (void)ranks; (void)n_ranks; (void)splits; (void)stream;
+    return fail(ORIGAMI_ERR_INVALID, "partition entry point not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,195 @@
+// Shared device-side definitions: item traits, shared-memory layout and the
+// merge primitives every kernel is built from.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace origami {
+
+// 16-byte key-value item, same layout as the reference's packed
+// KeyValue<i64,i64> (commons.h:51-72): key first, then value.
+struct __align__(16) KV64 {
+    uint64_t key;
+    uint64_t value;
+};
+
+// Keys are compared as unsigned integers. Signed 64-bit keys (the reference's
+// i64 and KeyValue<i64,i64>) are mapped onto the same order by flipping the sign
+// bit when an item is first read from the caller's buffer and flipping it back
+// when the final pass writes it: k -> k ^ 2^63 is an order-preserving bijection
+// from int64 to uint64.
+template <class T>
+struct Traits;
+
+template <>
+struct Traits<uint32_t> {
+    using Key = uint32_t;
+    static __host__ __device__ __forceinline__ Key key(uint32_t v) { return v; }
+    static __device__ __forceinline__ uint32_t flip(uint32_t v, uint64_t x) { return v ^ (uint32_t)x; }
+    static __device__ __forceinline__ uint32_t max_item() { return 0xFFFFFFFFu; }
+};
+
+template <>
+struct Traits<uint64_t> {
+    using Key = uint64_t;
+    static __host__ __device__ __forceinline__ Key key(uint64_t v) { return v; }
+    static __device__ __forceinline__ uint64_t flip(uint64_t v, uint64_t x) { return v ^ x; }
+    static __device__ __forceinline__ uint64_t max_item() { return ~0ull; }
+};
+
+template <>
+struct Traits<KV64> {
+    using Key = uint64_t;
+    static __host__ __device__ __forceinline__ Key key(const KV64& v) { return v.key; }
+    static __device__ __forceinline__ KV64 flip(KV64 v, uint64_t x) {
+        v.key ^= x;
+        return v;
+    }
+    static __device__ __forceinline__ KV64 max_item() { return KV64{~0ull, ~0ull}; }
+};
+
+template <class T>
+__device__ __forceinline__ bool less(const T& a, const T& b) {
+    return Traits<T>::key(a) < Traits<T>::key(b);
+}
+
+// Shared-memory index padding: one spare item after every 128 bytes, so that a
+// warp storing VT consecutive items per thread (blocked layout, VT a power of
+// two) hits distinct banks.
+template <class T>
+__host__ __device__ constexpr int pad_stride() {
+    return 128 / (int)sizeof(T);
+}
+template <class T>
+__host__ __device__ __forceinline__ int pad(int i) {
+    return i + i / pad_stride<T>();
+}
+template <class T>
+__host__ __device__ constexpr int padded_items(int n) {
+    return n + n / pad_stride<T>() + 1;
+}
+
+// Compare-exchange into ascending order.
+template <class T>
+__device__ __forceinline__ void cx(T& a, T& b) {
+    const bool sw = less(b, a);
+    const T lo = sw ? b : a;
+    const T hi = sw ? a : b;
+    a = lo;
+    b = hi;
+}
+template <>
+__device__ __forceinline__ void cx<uint32_t>(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b);
+    b = max(a, b);
+    a = lo;
+}
+template <>
+__device__ __forceinline__ void cx<uint64_t>(uint64_t& a, uint64_t& b) {
+    const uint64_t lo = min(a, b);
+    b = max(a, b);
+    a = lo;
+}
+
+// In-thread sort of VT register items, every aligned block of `chunk` items
+// (chunk a power of two) sorted independently.
+//  - keys only: bitonic network in the variant that leaves every merged block
+//    ascending (first stage of each merge compares i with i^(k-1)), so the
+//    network can stop at any block size;
+//  - stable (key-value): odd-even transposition, which only swaps neighbours
+//    that are strictly out of order and so keeps equal keys in input order.
+template <class T, int VT, bool STABLE>
+__device__ __forceinline__ void thread_sort(T (&v)[VT], int chunk) {
+    if constexpr (STABLE) {
+#pragma unroll
+        for (int r = 0; r < VT; ++r) {
+#pragma unroll
+            for (int i = r & 1; i + 1 < VT; i += 2) {
+                const bool same_chunk = (chunk >= VT) || (((i + 1) & (chunk - 1)) != 0);
+                if (same_chunk && less(v[i + 1], v[i])) {
+                    const T t = v[i];
+                    v[i] = v[i + 1];
+                    v[i + 1] = t;
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 2; k <= VT; k <<= 1) {
+            if (k <= chunk) {
+#pragma unroll
+                for (int i = 0; i < VT; ++i) {
+                    const int j = i ^ (k - 1);
+                    if (j > i) cx(v[i], v[j]);
+                }
+#pragma unroll
+                for (int s = k >> 2; s > 0; s >>= 1) {
+#pragma unroll
+                    for (int i = 0; i < VT; ++i) {
+                        const int j = i ^ s;
+                        if (j > i) cx(v[i], v[j]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Merge path (Odeh et al., "Merge Path - parallel merging made simple") over two
+// sorted lists held in padded shared memory: A = s[a0 .. a0+na), B = s[b0 .. b0+nb).
+// Returns how many of the first `diag` merged items come from A. A wins ties,
+// which makes every merge stable (A is always the earlier run).
+template <class T>
+__device__ __forceinline__ int smem_merge_path(const T* s, int a0, int na, int b0, int nb, int diag) {
+    int lo = max(0, diag - nb);
+    int hi = min(diag, na);
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const T a = s[pad<T>(a0 + mid)];
+        const T b = s[pad<T>(b0 + diag - 1 - mid)];
+        if (!less(b, a))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// The same search over global memory (used by the pass partition kernels).
+template <class T>
+__device__ __forceinline__ int64_t global_merge_path(const T* A, int64_t na, const T* B, int64_t nb,
+                                                     int64_t diag) {
+    int64_t lo = diag - nb > 0 ? diag - nb : 0;
+    int64_t hi = diag < na ? diag : na;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (!less(B[diag - 1 - mid], A[mid]))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Serial merge of VT outputs from A = s[ia..aEnd) and B = s[ib..bEnd) (padded
+// shared memory), A first on ties. One shared-memory load per output, selected
+// by predicate rather than a branch. Reads at most one item past either end.
+template <class T, int VT>
+__device__ __forceinline__ void smem_serial_merge(const T* s, int ia, int aEnd, int ib, int bEnd,
+                                                  T (&out)[VT]) {
+    T a = s[pad<T>(ia)];
+    T b = s[pad<T>(ib)];
+#pragma unroll
+    for (int k = 0; k < VT; ++k) {
+        const bool takeA = (ib >= bEnd) || (ia < aEnd && !less(b, a));
+        out[k] = takeA ? a : b;
+        if (k + 1 < VT) {
+            const int nxt = takeA ? ++ia : ++ib;
+            const T v = s[pad<T>(nxt)];
+            a = takeA ? v : a;
+            b = takeA ? b : v;
+        }
+    }
+}
+
+}  // namespace origami

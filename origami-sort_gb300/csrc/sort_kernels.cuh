@@ -1,0 +1,144 @@
+// The plain-sort kernels:
+//   K1 block_sort_kernel      - tile sort: registers (thread network) then
+//                               merge-path rounds in shared memory
+//   K4 pair_partition_kernel  - merge-path splitter search for one binary pass
+//   K3 pair_merge_kernel      - one output tile of a binary pass, staged in
+//                               shared memory and merged by merge path
+#pragma once
+#include "common.cuh"
+
+namespace origami {
+
+// ---------------------------------------------------------------- K1 -----
+// Sorts tiles of NT*VT items. Restates the reference's phase 1 + phase 2
+// (sorter.h:3831-3849: in-register networks, then binary merges up to the
+// in-cache block size) with the tile held in registers and shared memory.
+// `chunk` (power of two) caps the sorted run length for chunked sorts.
+// xin/xout are the key masks applied on load / on store (sign flip for i64).
+template <class T, int NT, int VT, bool STABLE>
+__global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in, T* __restrict__ out,
+                                                        uint64_t n, int chunk, uint64_t xin,
+                                                        uint64_t xout) {
+    constexpr int TILE = NT * VT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s = reinterpret_cast<T*>(smem_raw);
+    const int tid = threadIdx.x;
+    const uint64_t base = (uint64_t)blockIdx.x * TILE;
+    const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
+
+    // coalesced striped load; the tail of a partial tile is filled with the
+    // largest item, which sorts after every real item (stably for key-value)
+#pragma unroll
+    for (int k = 0; k < VT; ++k) {
+        const int i = k * NT + tid;
+        s[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
+    }
+    __syncthreads();
+    T v[VT];
+#pragma unroll
+    for (int k = 0; k < VT; ++k) v[k] = s[pad<T>(tid * VT + k)];
+    thread_sort<T, VT, STABLE>(v, chunk);
+
+    for (int w = VT; w < TILE && w < chunk; w <<= 1) {
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < VT; ++k) s[pad<T>(tid * VT + k)] = v[k];
+        __syncthreads();
+        const int o = tid * VT;
+        const int b0 = o & ~(2 * w - 1);
+        const int diag = o - b0;
+        const int a = smem_merge_path(s, b0, w, b0 + w, w, diag);
+        smem_serial_merge<T, VT>(s, b0 + a, b0 + w, b0 + w + diag - a, b0 + 2 * w, v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < VT; ++k) s[pad<T>(tid * VT + k)] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < VT; ++k) {
+        const int i = k * NT + tid;
+        if (i < valid) out[base + i] = Traits<T>::flip(s[pad<T>(i)], xout);
+    }
+}
+
+// Geometry of one binary pass: runs of `run` items (the last one may be short)
+// are merged pairwise (2p, 2p+1) into runs of 2*run. Output tiles of `tile`
+// items never straddle a pair because 2*run is a multiple of tile.
+struct PairGeom {
+    uint64_t pbase, la, lb;
+    __device__ __forceinline__ PairGeom(uint64_t o, uint64_t n, uint64_t run) {
+        pbase = (o / (2 * run)) * (2 * run);
+        const uint64_t rest = n - pbase;
+        la = rest < run ? rest : run;
+        lb = (rest - la) < run ? (rest - la) : run;
+    }
+};
+
+// ---------------------------------------------------------------- K4 -----
+// One thread per output-tile boundary: the merge-path split (items taken from
+// the left run) at the tile's first output. splits has num_tiles+1 entries.
+template <class T>
+__global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uint64_t run, int tile,
+                                      uint64_t num_tiles, int64_t* __restrict__ splits) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > num_tiles) return;
+    const uint64_t o = t * (uint64_t)tile < n ? t * (uint64_t)tile : n;
+    if (o >= n) {
+        splits[t] = 0;
+        return;
+    }
+    const PairGeom g(o, n, run);
+    const T* A = src + g.pbase;
+    splits[t] = global_merge_path(A, (int64_t)g.la, A + g.la, (int64_t)g.lb, (int64_t)(o - g.pbase));
+}
+
+// ---------------------------------------------------------------- K3 -----
+// Restates one level of the reference's binary merge (merger.h:4079-4218,
+// mergebl2_*) for one tile of output: the tile's slices of both runs are
+// staged in shared memory, every thread finds its diagonal by merge path and
+// merges VT items serially, and the tile is written back coalesced.
+template <class T, int NT, int VT>
+__global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
+                                                        uint64_t n, uint64_t run,
+                                                        const int64_t* __restrict__ splits,
+                                                        uint64_t xout) {
+    constexpr int TILE = NT * VT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s = reinterpret_cast<T*>(smem_raw);
+    const int tid = threadIdx.x;
+    const uint64_t t = blockIdx.x;
+    const uint64_t o = t * TILE;
+    const PairGeom g(o, n, run);
+    const uint64_t d0 = o - g.pbase;
+    const uint64_t pair_end = g.la + g.lb;
+    const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
+    const int64_t a0 = splits[t];
+    const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
+    const int64_t b0 = (int64_t)d0 - a0;
+    const int64_t b1 = (int64_t)d1 - a1;
+    const int na = (int)(a1 - a0);
+    const int nb = (int)(b1 - b0);
+    const int total = na + nb;
+    const T* A = src + g.pbase + a0;
+    const T* B = src + g.pbase + g.la + b0;
+
+    for (int i = tid; i < total; i += NT) s[pad<T>(i)] = (i < na) ? A[i] : B[i - na];
+    __syncthreads();
+
+    T v[VT];
+    const int diag = tid * VT;
+    if (diag < total) {
+        const int a = smem_merge_path(s, 0, na, na, nb, diag);
+        smem_serial_merge<T, VT>(s, a, na, na + diag - a, total, v);
+    }
+    __syncthreads();
+    if (diag < total) {
+#pragma unroll
+        for (int k = 0; k < VT; ++k) s[pad<T>(diag + k)] = v[k];
+    }
+    __syncthreads();
+    T* out = dst + o;
+    for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(s[pad<T>(i)], xout);
+}
+
+}  // namespace origami

@@ -1,0 +1,202 @@
+"""Python host-side mirror of the Origami sorter surface over the C ABI
+(include/origami_gpu.h, lib/liborigami_gpu.so).
+
+Names and argument meaning follow the reference's C++ entry points:
+
+    sort_single_thread(d, tmp_buf, sort_n, min_k)   sorter.h:3851-3915
+    sort_multi_thread(d, out, n_threads, n_cores, min_k, kway_buf)
+                                                    sorter.h:4194-4287
+    merge_series(src, dst, merge_start, sort_n)     merger.h:4220-4228
+
+Each returns whichever of its two buffers holds the sorted output, like the
+reference. Buffers are numpy arrays (host memory: staged through the device
+arena) or CUDA torch tensors (device memory: sorted in place, no copies).
+Errors raise OrigamiError carrying the library's status code; there is no CPU
+fallback - if the library is missing the import fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "liborigami_gpu.so")
+
+U32, U64, I64, KV64, KVU64 = 0, 1, 2, 3, 4
+KIND_NAMES = {"u32": U32, "u64": U64, "i64": I64, "kv64": KV64, "kvu64": KVU64}
+KV_DTYPE = np.dtype([("key", "<i8"), ("value", "<i8")])
+KVU_DTYPE = np.dtype([("key", "<u8"), ("value", "<u8")])
+ITEM_BYTES = {U32: 4, U64: 8, I64: 8, KV64: 16, KVU64: 16}
+
+OK = 0
+ERR_INVALID, ERR_ALIGN, ERR_OOM, ERR_CUDA, ERR_TIMEOUT = -1, -2, -3, -4, -5
+ERR_DTYPE, ERR_NO_DEVICE, ERR_BUSY, ERR_CANCELLED = -6, -7, -8, -9
+FLAG_RESULT_IN_TMP, FLAG_SYNC = 0x1, 0x2
+
+
+class OrigamiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"origami error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python origami-sort_gb300/build.py`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u64, ui, i = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint, ctypes.c_int
+        L.origami_version.restype = i
+        L.origami_last_error.restype = ctypes.c_char_p
+        L.origami_item_bytes.restype = ui
+        L.origami_item_bytes.argtypes = [i]
+        L.origami_sort.restype = i
+        L.origami_sort.argtypes = [i, vp, vp, u64, u64, ui, i, ctypes.POINTER(vp)]
+        L.origami_sort_device.restype = i
+        L.origami_sort_device.argtypes = [i, vp, vp, u64, u64, ui, i, ctypes.POINTER(vp), vp]
+        L.origami_merge_series_device.restype = i
+        L.origami_merge_series_device.argtypes = [i, vp, vp, u64, u64, u64, ctypes.POINTER(vp), vp]
+        L.origami_merge_tree_device.restype = i
+        L.origami_merge_tree_device.argtypes = [i, ctypes.POINTER(vp), ctypes.POINTER(vp), vp, ui, vp]
+        L.origami_partition_device.restype = i
+        L.origami_partition_device.argtypes = [i, ctypes.POINTER(vp), ctypes.POINTER(vp), ui,
+                                               ctypes.POINTER(u64), u64, ctypes.POINTER(u64), vp]
+        L.origami_arena_reserve.restype = i
+        L.origami_arena_reserve.argtypes = [u64]
+        L.origami_arena_trim.restype = i
+        L.origami_arena_bytes_in_use.restype = u64
+        L.origami_profile_enable.restype = i
+        L.origami_profile_enable.argtypes = [i]
+        L.origami_profile_report.restype = i
+        L.origami_profile_report.argtypes = [ctypes.c_char_p, u64]
+        L.origami_launch_count.restype = u64
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != OK:
+        raise OrigamiError(rc, lib().origami_last_error().decode(errors="replace"))
+    return rc
+
+
+def kind_of_dtype(dt):
+    dt = np.dtype(dt)
+    if dt == np.uint32:
+        return U32
+    if dt == np.uint64:
+        return U64
+    if dt == np.int64:
+        return I64
+    if dt == KV_DTYPE:
+        return KV64
+    if dt == KVU_DTYPE:
+        return KVU64
+    raise OrigamiError(ERR_DTYPE, f"unsupported item dtype {dt}")
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr_len(x, kind):
+    if x is None:
+        return None, 0
+    if _is_torch(x):
+        return x.data_ptr(), x.numel() * x.element_size() // ITEM_BYTES[kind]
+    return x.ctypes.data, len(x)
+
+
+def _kind(d, kind):
+    if kind is not None:
+        return KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    if _is_torch(d):
+        raise OrigamiError(ERR_DTYPE, "pass kind= for torch tensors (u32/u64/i64/kv64/kvu64)")
+    return kind_of_dtype(d.dtype)
+
+
+def sort(d, tmp=None, sort_n=0, min_k=0, kind=None, result_in_tmp=False, stream=None):
+    """Sort d (chunked by sort_n). Returns d or tmp, whichever holds the output.
+
+    Host (numpy) buffers block until the result is back in host memory. CUDA
+    tensors are sorted on `stream` (default: torch's current stream) and the
+    call returns once the work is enqueued."""
+    k = _kind(d, kind)
+    dp, n = _ptr_len(d, k)
+    tp, _ = _ptr_len(tmp, k)
+    res = ctypes.c_void_p()
+    flags = FLAG_RESULT_IN_TMP if result_in_tmp else 0
+    if _is_torch(d):
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(d.device).cuda_stream
+        check(lib().origami_sort_device(k, dp, tp, n, sort_n, min_k, flags, ctypes.byref(res),
+                                        ctypes.c_void_p(s)))
+    else:
+        check(lib().origami_sort(k, dp, tp, n, sort_n, min_k, flags, ctypes.byref(res)))
+    if n == 0:
+        return d
+    return tmp if (tmp is not None and res.value == tp) else d
+
+
+def sort_single_thread(d, tmp_buf, sort_n=0, min_k=2, interim_buf=None, kind=None):
+    """origami_sorter::sort_single_thread (sorter.h:3851-3915) on the GPU."""
+    del interim_buf  # the GPU merge tree keeps its buffers on chip
+    return sort(d, tmp_buf, sort_n, min_k, kind=kind)
+
+
+def sort_multi_thread(d, out, n_threads=1, n_cores=1, min_k=2, kway_buf=None, kind=None):
+    """origami_sorter::sort_multi_thread (sorter.h:4194-4287): the whole GPU is
+    used; the thread arguments are accepted for compatibility and ignored."""
+    del n_threads, n_cores, kway_buf
+    return sort(d, out, 0, min_k, kind=kind)
+
+
+def merge_series(src, dst, merge_start, sort_n, kind=None, stream=None):
+    """origami_merger::merge_series (merger.h:4220-4228) on CUDA tensors."""
+    import torch
+    k = _kind(src, kind)
+    sp, n = _ptr_len(src, k)
+    dp, _ = _ptr_len(dst, k)
+    res = ctypes.c_void_p()
+    s = stream if stream is not None else torch.cuda.current_stream(src.device).cuda_stream
+    check(lib().origami_merge_series_device(k, sp, dp, n, merge_start, sort_n, ctypes.byref(res),
+                                            ctypes.c_void_p(s)))
+    return dst if res.value == dp else src
+
+
+def profile_enable(on=True):
+    check(lib().origami_profile_enable(1 if on else 0))
+
+
+def profile_report():
+    """{kernel: (launches, total_ms)} for the launches since profile_enable()."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    rc = lib().origami_profile_report(buf, len(buf))
+    if rc < 0:
+        check(rc)
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.rsplit(",", 2)
+        out[name] = (int(cnt), float(ms))
+    return out
+
+
+def launch_count():
+    return int(lib().origami_launch_count())
+
+
+def empty_host(kind, n, pinned=False):
+    """Host buffer for n items of `kind` (numpy; page-locked when pinned=True)."""
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    dt = {U32: np.dtype(np.uint32), U64: np.dtype(np.uint64), I64: np.dtype(np.int64),
+          KV64: KV_DTYPE, KVU64: KVU_DTYPE}[k]
+    if pinned:
+        import torch
+        t = torch.empty(n * dt.itemsize, dtype=torch.uint8, pin_memory=True)
+        return t.numpy().view(dt)  # the array's base chain keeps the pinned tensor alive
+    return np.empty(n, dt)

@@ -1,0 +1,82 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol
+include/origami_gpu.h declares, and rejects bad arguments with the documented
+status codes before touching a device."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import origami_gpu as og
+
+HDR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+
+
+def declared_symbols():
+    syms = set()
+    for f in os.listdir(HDR):
+        if f.endswith(".h"):
+            text = open(os.path.join(HDR, f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            syms |= set(re.findall(r"\b(origami_\w+)\s*\(", text))
+    return sorted(syms)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as g
+    g.build_library()
+    return og.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), f"{s} declared in include/ but not exported"
+
+
+def test_version_and_item_bytes(lib):
+    assert lib.origami_version() >= 100
+    assert [lib.origami_item_bytes(k) for k in range(5)] == [4, 8, 8, 16, 16]
+    assert lib.origami_item_bytes(99) == 0
+
+
+def _call(kind, d, tmp, n, sort_n=0, flags=0):
+    res = ctypes.c_void_p()
+    return og.lib().origami_sort(kind, d, tmp, n, sort_n, 0, flags, ctypes.byref(res))
+
+
+def test_rejects_bad_arguments(lib):
+    a = np.zeros(64, np.uint32)
+    b = np.zeros(64, np.uint32)
+    assert _call(9, a.ctypes.data, b.ctypes.data, 64) == og.ERR_DTYPE
+    assert _call(0, None, b.ctypes.data, 64) == og.ERR_INVALID
+    # sort_n must be 0, >= n or a power of two
+    assert _call(0, a.ctypes.data, b.ctypes.data, 64, sort_n=12) == og.ERR_INVALID
+    # overlapping buffers
+    assert _call(0, a.ctypes.data, a.ctypes.data + 16, 64) == og.ERR_INVALID
+    # misaligned pointer
+    assert _call(0, a.ctypes.data + 1, b.ctypes.data, 8) == og.ERR_ALIGN
+    # a NULL result pointer
+    assert og.lib().origami_sort(0, a.ctypes.data, b.ctypes.data, 64, 0, 0, 0, None) == og.ERR_INVALID
+    assert b"sort_n" in og.lib().origami_last_error() or og.lib().origami_last_error()
+
+
+def test_no_device_is_reported_not_crashed(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    a = np.arange(100, dtype=np.uint32)[::-1].copy()
+    b = np.zeros(100, np.uint32)
+    assert _call(0, a.ctypes.data, b.ctypes.data, 100) == og.ERR_NO_DEVICE
+
+
+def test_python_surface_raises_without_fallback(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(og.OrigamiError) as e:
+        og.sort_single_thread(np.arange(10, dtype=np.uint32), np.zeros(10, np.uint32))
+    assert e.value.code == og.ERR_NO_DEVICE
