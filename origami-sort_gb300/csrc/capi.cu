@@ -56,16 +56,12 @@ void prof_end(int slot, cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
     cudaEventRecord(g_recs[slot].b, st);
 }
-uint64_t split_slots_u32(uint64_t n);
-uint64_t split_slots_u64(uint64_t n);
-uint64_t split_slots_kv(uint64_t n);
-
-uint64_t split_slots(int kind, uint64_t n) {
+uint64_t scratch_bytes(int kind, uint64_t n, uint64_t sort_n, int fan) {
     switch (kind) {
-        case ORIGAMI_U32: return split_slots_u32(n);
+        case ORIGAMI_U32: return scratch_bytes_u32(n, sort_n, fan);
         case ORIGAMI_U64:
-        case ORIGAMI_I64: return split_slots_u64(n);
-        default: return split_slots_kv(n);
+        case ORIGAMI_I64: return scratch_bytes_u64(n, sort_n, fan);
+        default: return scratch_bytes_kv(n, sort_n, fan);
     }
 }
 }  // namespace origami
@@ -175,20 +171,30 @@ int check_args(int kind, const void* d, const void* tmp, uint64_t n, uint64_t so
     return ORIGAMI_OK;
 }
 
+// Merge fan-in for a min_k request: 2 keeps binary passes, 3..16 round up to
+// a power of two, larger values are capped at 16; 0 selects the default.
+int fan_of(unsigned min_k) {
+    if (min_k == 0) return 16;
+    if (min_k <= 2) return 2;
+    int f = 4;
+    while ((unsigned)f < min_k && f < 16) f <<= 1;
+    return f;
+}
+
 cudaError_t run_typed(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, void* want,
-                      int64_t* splits, cudaStream_t st) {
+                      int fan, void* scratch, cudaStream_t st) {
     const uint64_t m = key_mask(kind);
     switch (kind) {
-        case ORIGAMI_U32: return sort_u32(d, tmp, n, sort_n, m, want, splits, st, nullptr);
+        case ORIGAMI_U32: return sort_u32(d, tmp, n, sort_n, m, want, fan, scratch, st, nullptr);
         case ORIGAMI_U64:
-        case ORIGAMI_I64: return sort_u64(d, tmp, n, sort_n, m, want, splits, st, nullptr);
-        default: return sort_kv(d, tmp, n, sort_n, m, want, splits, st, nullptr);
+        case ORIGAMI_I64: return sort_u64(d, tmp, n, sort_n, m, want, fan, scratch, st, nullptr);
+        default: return sort_kv(d, tmp, n, sort_n, m, want, fan, scratch, st, nullptr);
     }
 }
 
 // Device-resident sort; the caller has validated the arguments.
-int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, int flags,
-                     void** result, cudaStream_t st) {
+int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                     int flags, void** result, cudaStream_t st) {
     const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
     if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
     *result = in_tmp ? tmp : d;
@@ -200,14 +206,15 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
     }
     void* scratch = nullptr;
     if (!tmp) CK(cudaMallocAsync(&scratch, n * item_bytes(kind), st), "scratch allocation");
-    int64_t* splits = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&splits, split_slots(kind, n) * sizeof(int64_t), st);
+    const int fan = fan_of(min_k);
+    void* work = nullptr;
+    cudaError_t e = cudaMallocAsync(&work, scratch_bytes(kind, n, sort_n, fan), st);
     if (e != cudaSuccess) {
         if (scratch) cudaFreeAsync(scratch, st);
         return cuda_fail(e, "splitter allocation");
     }
-    e = run_typed(kind, d, tmp ? tmp : scratch, n, sort_n, in_tmp ? tmp : d, splits, st);
-    cudaFreeAsync(splits, st);
+    e = run_typed(kind, d, tmp ? tmp : scratch, n, sort_n, in_tmp ? tmp : d, fan, work, st);
+    cudaFreeAsync(work, st);
     if (scratch) cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(e, "sort launch");
     if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
@@ -216,8 +223,8 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
 
 // Host buffers: stage through the arena, sort on the device, copy the result
 // back into d (or tmp) and return when it is there.
-int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, int flags,
-                   void** result) {
+int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
+                   int flags, void** result) {
     const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
     if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
     void* out = in_tmp ? tmp : d;
@@ -237,7 +244,7 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, in
     void* dres = nullptr;
     e = cudaMemcpyAsync(dd, d, bytes, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        rc = sort_device_impl(kind, dd, dt, n, sort_n, 0, &dres, st);
+        rc = sort_device_impl(kind, dd, dt, n, sort_n, min_k, 0, &dres, st);
         if (rc == ORIGAMI_OK) e = cudaMemcpyAsync(out, dres, bytes, cudaMemcpyDeviceToHost, st);
     }
     cudaFreeAsync(dd, st);
@@ -261,11 +268,10 @@ unsigned origami_item_bytes(int kind) { return valid_kind(kind) ? item_bytes(kin
 
 int origami_sort_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
                         int flags, void** result, void* stream) {
-    (void)min_k;
     int rc = check_args(kind, d, tmp, n, sort_n, result);
     if (rc != ORIGAMI_OK) return rc;
     if ((rc = ensure_device()) != ORIGAMI_OK) return rc;
-    return sort_device_impl(kind, d, tmp, n, sort_n, flags, result, (cudaStream_t)stream);
+    return sort_device_impl(kind, d, tmp, n, sort_n, min_k, flags, result, (cudaStream_t)stream);
 }
 
 int origami_sort(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
@@ -273,13 +279,12 @@ int origami_sort(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsi
     int rc = check_args(kind, d, tmp, n, sort_n, result);
     if (rc != ORIGAMI_OK) return rc;
     if ((rc = ensure_device()) != ORIGAMI_OK) return rc;
-    (void)min_k;
     if (n > 0 && is_device_pointer(d)) {
         if (tmp && !is_device_pointer(tmp))
             return fail(ORIGAMI_ERR_INVALID, "d is device memory but tmp is not");
-        return sort_device_impl(kind, d, tmp, n, sort_n, flags | ORIGAMI_FLAG_SYNC, result, 0);
+        return sort_device_impl(kind, d, tmp, n, sort_n, min_k, flags | ORIGAMI_FLAG_SYNC, result, 0);
     }
-    return sort_host_impl(kind, d, tmp, n, sort_n, flags, result);
+    return sort_host_impl(kind, d, tmp, n, sort_n, min_k, flags, result);
 }
 
 #define ORIGAMI_TYPED(name, KIND)                                                                  \
@@ -313,7 +318,7 @@ int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint
     const int flags = (levels & 1) ? ORIGAMI_FLAG_RESULT_IN_TMP : 0;
     // Merging sorted runs stably up to sort_n gives exactly the stable chunk
     // sort of the input, which is what the pipeline computes.
-    return sort_device_impl(kind, src, dst, n, sort_n, flags, result, (cudaStream_t)stream);
+    return sort_device_impl(kind, src, dst, n, sort_n, 2, flags, result, (cudaStream_t)stream);
 }
 
 int origami_arena_reserve(uint64_t bytes) {

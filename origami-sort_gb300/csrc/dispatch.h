@@ -8,14 +8,16 @@ namespace origami {
 
 struct LaunchStats;
 
-// Sorts d[0..n) in chunks of sort_n into `want` (d or tmp); see pipeline.cuh.
-cudaError_t sort_u32(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, void* want,
-                     int64_t* splits, cudaStream_t st, LaunchStats* stats);
-cudaError_t sort_u64(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, void* want,
-                     int64_t* splits, cudaStream_t st, LaunchStats* stats);
-cudaError_t sort_kv(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, void* want,
-                    int64_t* splits, cudaStream_t st, LaunchStats* stats);
-// int64 slots the splitter scratch needs for n items of the given kind.
-uint64_t split_slots(int kind, uint64_t n);
+// Sorts d[0..n) in chunks of sort_n into `want` (d or tmp) with merge fan-in
+// `fan` (2 = binary passes, 4/8/16 = k-way passes); see pipeline.cuh.
+#define ORIGAMI_DECLARE_SORT(name)                                                              \
+    cudaError_t sort_##name(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, \
+                            void* want, int fan, void* scratch, cudaStream_t st,                \
+                            LaunchStats* stats);                                                \
+    uint64_t scratch_bytes_##name(uint64_t n, uint64_t sort_n, int fan);
+ORIGAMI_DECLARE_SORT(u32)
+ORIGAMI_DECLARE_SORT(u64)
+ORIGAMI_DECLARE_SORT(kv)
+#undef ORIGAMI_DECLARE_SORT
 
 }  // namespace origami

@@ -1,0 +1,386 @@
+// k-way merge passes (fan-in F <= 16): the GPU form of the reference's
+// cache-resident merge tree (merge_tree.h: Merge4Way nodes, MergeTreeEven/Odd)
+// and its parallel partitioner (Partition.h:118-166).
+//
+// One pass merges groups of F consecutive sorted runs. Work is cut in two
+// levels, both exact and skew-proof:
+//  * ranges  - kway_split_kernel (K4) computes, for evenly spaced output ranks
+//              of a group, the exact split of every run (merge path in k
+//              dimensions: all runs bisected together, see below);
+//  * tiles   - inside a range, range_merge_kernel (K3) takes every S-th item of
+//              each run as a sample, merges the samples in shared memory and
+//              cuts the range at every m-th merged sample. A cut at a concrete
+//              item is exact by construction (its split in run j is one short
+//              binary search in an S-item block) and bounds every tile to at
+//              most (m + F) * S items, whatever the key distribution.
+// Each tile's F slices are staged in shared memory and merged by log2(F)
+// rounds of merge path, so one HBM read + write covers log2(F) merge levels.
+//
+// Ties: items are ordered by (key, run index, position), which makes the merge
+// stable across runs and gives every item exactly one place.
+#pragma once
+#include "common.cuh"
+
+namespace origami {
+
+constexpr int KWAY_MAX = 16;
+
+// ------------------------------------------------------------ samples ----
+template <class K>
+struct SampleE {
+    K key;
+    uint32_t tag;  // (index in run) << 4 | run
+};
+template <class K>
+__device__ __forceinline__ bool less(const SampleE<K>& a, const SampleE<K>& b) {
+    return a.key < b.key;
+}
+
+// Merge `nl` (a power of two <= 16) sorted lists held back to back in padded
+// shared memory (list i = src[off[i] .. off[i+1]), off[nl] == tot) into one list.
+// Each round merges adjacent pairs by merge path; the lower-indexed list wins
+// ties in every round, so the result is ordered by (key, list index). `off` is
+// rewritten. Returns the buffer holding the result (src or dst). Must be called
+// by all NT threads of the block.
+template <class E, int NT, int VT>
+__device__ E* smem_merge_lists(E* src, E* dst, int* off, int nl, int tot) {
+    const int tid = threadIdx.x;
+    while (nl > 1) {
+        const int npairs = nl >> 1;
+        for (int k0 = tid * VT; k0 < tot; k0 += NT * VT) {
+            int k = k0;
+            const int kend = min(k0 + VT, tot);
+            while (k < kend) {
+                // the pair holding output k: the last pair starting at or before k
+                int p = 0;
+                for (int q = 1; q < npairs; ++q)
+                    if (off[2 * q] <= k) p = q;
+                const int a0 = off[2 * p], b0 = off[2 * p + 1], e0 = off[2 * p + 2];
+                const int diag = k - a0;
+                const int a = smem_merge_path(src, a0, b0 - a0, b0, e0 - b0, diag);
+                const int cnt = min(kend, e0) - k;
+                int ia = a0 + a, ib = b0 + diag - a;
+                E x = src[pad<E>(ia)];
+                E y = src[pad<E>(ib)];
+#pragma unroll
+                for (int i = 0; i < VT; ++i) {
+                    if (i < cnt) {
+                        const bool takeA = (ib >= e0) || (ia < b0 && !less(y, x));
+                        dst[pad<E>(k + i)] = takeA ? x : y;
+                        const int nxt = takeA ? ++ia : ++ib;
+                        const E v = src[pad<E>(nxt)];
+                        x = takeA ? v : x;
+                        y = takeA ? y : v;
+                    }
+                }
+                k += cnt;
+            }
+        }
+        __syncthreads();
+        if (tid == 0)
+            for (int q = 0; q <= npairs; ++q) off[q] = off[2 * q];
+        __syncthreads();
+        E* t = src;
+        src = dst;
+        dst = t;
+        nl = npairs;
+    }
+    return src;
+}
+
+// ------------------------------------------------------- K4: ranges ------
+// Exact split of a group of runs at output rank r: for every run i the number
+// s_i of its items among the r smallest of the group. One 256-thread block per
+// split; thread (j, i) = (tid / 16, tid % 16).
+//
+// All runs are bisected together. Each round every run j with an open window
+// [lo_j, hi_j) offers its middle item x_j as a probe; lane (j, i) counts the
+// items of run i that precede x_j, clamped to run i's window (one binary search
+// in the window). The clamped counts sum to less than r exactly when x_j is
+// among the r smallest, which moves every window: lo_i up to the count under a
+// probe on the left, hi_i down to the count under a probe on the right. Run
+// j's own window at least halves each round, so the loop ends after at most
+// ~log2(run) + 1 rounds with lo_i == hi_i == s_i for all i.
+struct SplitGeom {
+    uint64_t base, G;
+    int nr;
+    __device__ __forceinline__ SplitGeom(uint64_t g, uint64_t n, uint64_t run, int F) {
+        base = g * run * (uint64_t)F;
+        const uint64_t rest = n - base;
+        G = rest < run * (uint64_t)F ? rest : run * (uint64_t)F;
+        nr = (int)((G + run - 1) / run);
+    }
+    __device__ __forceinline__ uint64_t len(int i, uint64_t run) const {
+        const uint64_t s = (uint64_t)i * run;
+        return (i < nr) ? ((G - s) < run ? (G - s) : run) : 0;
+    }
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ src, uint64_t n,
+                                                         uint64_t run, int F, int rpg,
+                                                         int64_t* __restrict__ bnd,
+                                                         int* __restrict__ err) {
+    using K = typename Traits<T>::Key;
+    __shared__ int64_t lo[KWAY_MAX], hi[KWAY_MAX];
+    __shared__ unsigned long long nlo[KWAY_MAX], nhi[KWAY_MAX];
+    __shared__ int open;
+    const int tid = threadIdx.x;
+    const uint64_t g = blockIdx.x / (uint64_t)(rpg + 1);
+    const int b = (int)(blockIdx.x % (uint64_t)(rpg + 1));
+    const SplitGeom geo(g, n, run, F);
+    const uint64_t r = (uint64_t)(((unsigned __int128)b * geo.G) / (uint64_t)rpg);
+    int64_t* out = bnd + (uint64_t)blockIdx.x * KWAY_MAX;
+    if (tid < KWAY_MAX) {
+        const int64_t L = (int64_t)geo.len(tid, run);
+        const int64_t others = (int64_t)geo.G - L;
+        lo[tid] = (int64_t)r - others > 0 ? (int64_t)r - others : 0;
+        hi[tid] = (int64_t)r < L ? (int64_t)r : L;
+    }
+    __syncthreads();
+    const int j = tid >> 4, i = tid & 15;
+    const T* runj = src + geo.base + (uint64_t)j * run;
+    const T* runi = src + geo.base + (uint64_t)i * run;
+    for (int round = 0; round < 80; ++round) {
+        if (tid == 0) {
+            int o = 0;
+            for (int q = 0; q < KWAY_MAX; ++q) o |= (lo[q] < hi[q]);
+            open = o;
+        }
+        if (tid < KWAY_MAX) {
+            nlo[tid] = (unsigned long long)lo[tid];
+            nhi[tid] = (unsigned long long)hi[tid];
+        }
+        __syncthreads();
+        if (!open) break;
+        const int64_t loj = lo[j], hij = hi[j];
+        const bool probe = (j < geo.nr) && (loj < hij);
+        const int64_t pj = loj + (hij - loj) / 2;
+        K xk = 0;
+        if (probe && i == j) xk = Traits<T>::key(runj[pj]);
+        xk = __shfl_sync(0xFFFFFFFFu, xk, (tid & 16) | j);
+        int64_t c = 0;
+        if (probe && i < geo.nr) {
+            if (i == j) {
+                c = pj;
+            } else {
+                int64_t a = lo[i], e = hi[i];
+                const bool le = i < j;  // earlier runs precede on equal keys
+                while (a < e) {
+                    const int64_t mid = (a + e) >> 1;
+                    const K v = Traits<T>::key(runi[mid]);
+                    if (le ? (v <= xk) : (v < xk))
+                        a = mid + 1;
+                    else
+                        e = mid;
+                }
+                c = a;
+            }
+        }
+        // sum over i within the 16-lane group
+        int64_t sum = c;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+        if (probe && i < geo.nr) {
+            if ((uint64_t)sum < r)
+                atomicMax(&nlo[i], (unsigned long long)(i == j ? pj + 1 : c));
+            else
+                atomicMin(&nhi[i], (unsigned long long)(i == j ? pj : c));
+        }
+        __syncthreads();
+        if (tid < KWAY_MAX) {
+            lo[tid] = (int64_t)nlo[tid];
+            hi[tid] = (int64_t)nhi[tid];
+        }
+        __syncthreads();
+        if (round == 79 && tid == 0) atomicExch(err, 1);  // cannot happen: windows halve
+    }
+    if (tid < KWAY_MAX) out[tid] = lo[tid];
+}
+
+// ------------------------------------------------------- K3: ranges ------
+template <class T>
+struct KwayCfg;
+template <>
+struct KwayCfg<uint32_t> {
+    static constexpr int NT = 512, VT = 16, S = 64, TMAX = 9216;
+    static constexpr int RANGE = 1 << 18;
+};
+template <>
+struct KwayCfg<uint64_t> {
+    static constexpr int NT = 512, VT = 8, S = 64, TMAX = 5120;
+    static constexpr int RANGE = 1 << 17;
+};
+template <>
+struct KwayCfg<KV64> {
+    static constexpr int NT = 256, VT = 8, S = 32, TMAX = 2560;
+    static constexpr int RANGE = 1 << 16;
+};
+
+template <class T>
+struct KwayLayout {
+    using C = KwayCfg<T>;
+    using K = typename Traits<T>::Key;
+    using E = SampleE<K>;
+    static constexpr int CAP_ITEMS = padded_items<T>(C::TMAX + 1);  // per buffer
+    static constexpr size_t BUF_BYTES = ((size_t)CAP_ITEMS * sizeof(T) + 15) & ~(size_t)15;
+    static constexpr int SCAP = (int)(BUF_BYTES / sizeof(E)) - (int)(BUF_BYTES / sizeof(E)) / pad_stride<E>() - 2;
+    static constexpr int M = C::TMAX / C::S - KWAY_MAX;  // merged samples per tile
+    static constexpr int MAXTILES = C::RANGE / (M * C::S) + 2;
+    static constexpr size_t SMEM = 2 * BUF_BYTES + (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + 256;
+    static_assert(C::RANGE / C::S <= SCAP, "range samples must fit one buffer");
+};
+
+// One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
+template <class T>
+__global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
+    const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int F, int rpg,
+    const int64_t* __restrict__ bnd, uint64_t xout) {
+    using C = KwayCfg<T>;
+    using Lay = KwayLayout<T>;
+    using K = typename Traits<T>::Key;
+    using E = SampleE<K>;
+    constexpr int NT = C::NT, VT = C::VT, S = C::S, M = Lay::M;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* bufA = reinterpret_cast<T*>(smem_raw);
+    T* bufB = reinterpret_cast<T*>(smem_raw + Lay::BUF_BYTES);
+    uint32_t* sp = reinterpret_cast<uint32_t*>(smem_raw + 2 * Lay::BUF_BYTES);  // [MAXTILES+1][16]
+    uint32_t* hist = sp + (Lay::MAXTILES + 1) * KWAY_MAX;                      // [MAXTILES+1][16]
+    __shared__ int off[KWAY_MAX + 1];
+    __shared__ int64_t lo[KWAY_MAX];
+    __shared__ uint32_t len[KWAY_MAX];
+    __shared__ uint64_t out_base;
+    __shared__ int ntiles;
+    const int tid = threadIdx.x;
+
+    // --- range geometry
+    const uint64_t g = bnd ? blockIdx.x / (uint64_t)rpg : blockIdx.x;
+    const int rb = bnd ? (int)(blockIdx.x % (uint64_t)rpg) : 0;
+    const SplitGeom geo(g, n, run, F);
+    if (tid < KWAY_MAX) {
+        const uint64_t L = geo.len(tid, run);
+        int64_t a = 0, e = (int64_t)L;
+        if (bnd) {
+            const int64_t* bb = bnd + ((uint64_t)g * (rpg + 1) + rb) * KWAY_MAX;
+            a = bb[tid];
+            e = bb[KWAY_MAX + tid];
+        }
+        lo[tid] = (int64_t)(geo.base + (uint64_t)tid * run) + a;
+        len[tid] = (uint32_t)(e - a);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t ob = geo.base;
+        for (int q = 0; q < KWAY_MAX; ++q) ob += (uint64_t)(lo[q] - (int64_t)(geo.base + (uint64_t)q * run));
+        out_base = ob;
+        int o = 0;
+        for (int q = 0; q < KWAY_MAX; ++q) {
+            off[q] = o;
+            o += (int)(len[q] / S);
+        }
+        off[KWAY_MAX] = o;
+    }
+    __syncthreads();
+    const int nsamp = off[KWAY_MAX];
+    const int nl = (geo.nr <= 1) ? 1 : (geo.nr <= 2 ? 2 : (geo.nr <= 4 ? 4 : (geo.nr <= 8 ? 8 : 16)));
+
+    // --- fine samples: the last item of every full S-block of every run
+    E* sA = reinterpret_cast<E*>(bufA);
+    E* sB = reinterpret_cast<E*>(bufB);
+    for (int q = 0; q < geo.nr; ++q) {
+        const int c = off[q + 1] - off[q];
+        const T* rp = src + lo[q];
+        for (int k = tid; k < c; k += NT) {
+            E e;
+            e.key = Traits<T>::key(rp[(uint64_t)(k + 1) * S - 1]);
+            e.tag = ((uint32_t)k << 4) | (uint32_t)q;
+            sA[pad<E>(off[q] + k)] = e;
+        }
+    }
+    // runs beyond nr hold no samples, so off[nr..16] == nsamp already
+    __syncthreads();
+    E* merged = sA;
+    if (nl > 1 && nsamp > 0) merged = smem_merge_lists<E, NT, VT>(sA, sB, off, nl, nsamp);
+
+    // --- tile cuts at merged samples M-1, 2M-1, ...
+    const int nt = nsamp / M + 1;
+    for (int q = tid; q < nt * KWAY_MAX; q += NT) hist[q] = 0;
+    __syncthreads();
+    for (int q = tid; q < nsamp; q += NT) atomicAdd(&hist[(q / M) * KWAY_MAX + (merged[pad<E>(q)].tag & 15)], 1u);
+    __syncthreads();
+    // prefix over tiles: P[b][j] = samples of run j at merged positions < b*M
+    if (tid < KWAY_MAX) {
+        uint32_t acc = 0;
+        for (int b = 0; b < nt; ++b) {
+            const uint32_t h = hist[b * KWAY_MAX + tid];
+            hist[b * KWAY_MAX + tid] = acc;
+            acc += h;
+        }
+        hist[nt * KWAY_MAX + tid] = acc;
+    }
+    __syncthreads();
+    // splits: sp[b][j] = items of run j (relative to lo[j]) at or before cut b
+    for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) {
+        const int b = q / KWAY_MAX, j = q % KWAY_MAX;
+        uint32_t v;
+        if (b == 0) {
+            v = 0;
+        } else if (b == nt || j >= geo.nr) {
+            v = (j < geo.nr) ? len[j] : 0;
+        } else {
+            const E gs = merged[pad<E>(b * M - 1)];
+            const int gi = (int)(gs.tag & 15);
+            const uint32_t pj = hist[b * KWAY_MAX + j];  // run-j samples at positions <= b*M-1
+            if (j == gi) {
+                v = pj * S;
+            } else {
+                uint32_t a = pj * S;
+                uint32_t e = min(a + (uint32_t)(S - 1), len[j]);
+                const T* rp = src + lo[j];
+                const bool le = j < gi;
+                while (a < e) {
+                    const uint32_t mid = (a + e) >> 1;
+                    const K kv = Traits<T>::key(rp[mid]);
+                    if (le ? (kv <= gs.key) : (kv < gs.key))
+                        a = mid + 1;
+                    else
+                        e = mid;
+                }
+                v = a;
+            }
+        }
+        sp[q] = v;
+    }
+    if (tid == 0) ntiles = nt;
+    __syncthreads();
+
+    // --- tiles
+    for (int t = 0; t < ntiles; ++t) {
+        if (tid == 0) {
+            int o = 0;
+            for (int q = 0; q < KWAY_MAX; ++q) {
+                off[q] = o;
+                o += (int)(sp[(t + 1) * KWAY_MAX + q] - sp[t * KWAY_MAX + q]);
+            }
+            off[KWAY_MAX] = o;
+        }
+        __syncthreads();
+        const int tot = off[KWAY_MAX];
+        for (int q = 0; q < geo.nr; ++q) {
+            const int l = off[q + 1] - off[q];
+            const T* rp = src + lo[q] + sp[t * KWAY_MAX + q];
+            const int o0 = off[q];
+            for (int k = tid; k < l; k += NT) bufA[pad<T>(o0 + k)] = rp[k];
+        }
+        __syncthreads();
+        T* res = bufA;
+        if (nl > 1) res = smem_merge_lists<T, NT, VT>(bufA, bufB, off, nl, tot);
+        uint64_t ob = out_base;
+        for (int q = 0; q < KWAY_MAX; ++q) ob += sp[t * KWAY_MAX + q];
+        T* op = dst + ob;
+        for (int k = tid; k < tot; k += NT) op[k] = Traits<T>::flip(res[pad<T>(k)], xout);
+        __syncthreads();
+    }
+}
+
+}  // namespace origami

@@ -8,6 +8,9 @@
 #include <string>
 #include <cuda_runtime.h>
 
+#include <vector>
+
+#include "kway.cuh"
 #include "profiler.h"
 #include "sort_kernels.cuh"
 
@@ -65,29 +68,91 @@ struct LaunchStats {
     int passes = 0;   // HBM passes (K1 + merge passes)
 };
 
-// Sorts d[0..n) in chunks of sort_n (0 = one full sort). The output lands in
-// `want` (d or tmp); `key_mask` is XORed into every key on the way in and out.
-// `splits` must hold merge_split_slots(n) int64 values (device memory).
+// int64 slots the binary-pass splitter array needs (one per merge tile + 1).
 template <class T>
 inline uint64_t merge_split_slots(uint64_t n) {
     return n / merge_tile<T>() + 2;
 }
 
+// One merge pass of the plan: runs of `run` items merged `fan` at a time.
+struct PassPlan {
+    uint64_t run;
+    int fan;          // 2 = binary pass (K4 pair partition + K3 pair merge)
+    uint64_t groups;  // k-way: groups of `fan` runs
+    int rpg;          // k-way: exact ranges per group (1 = the group is one range)
+};
+
+inline int next_pow2_int(uint64_t v) {
+    int p = 1;
+    while ((uint64_t)p < v && p < (1 << 30)) p <<= 1;
+    return p;
+}
+
+// The merge passes after K1 for runs to reach `limit` (chunk size or n).
+// fan == 2 gives the binary pipeline; fan in {4, 8, 16} the k-way one, whose
+// last pass uses the smallest fan-in that still reaches `limit`.
+template <class T>
+std::vector<PassPlan> plan_passes(uint64_t n, uint64_t limit, int fan) {
+    std::vector<PassPlan> v;
+    uint64_t run = k1_tile<T>();
+    while (run < limit) {
+        PassPlan p{run, 2, 0, 1};
+        if (fan > 2) {
+            const uint64_t need = (limit + run - 1) / run;
+            p.fan = need < (uint64_t)fan ? next_pow2_int(need) : fan;
+            if (p.fan < 2) p.fan = 2;
+            const uint64_t G = run * (uint64_t)p.fan;
+            p.groups = (n + G - 1) / G;
+            const uint64_t R = KwayCfg<T>::RANGE;
+            p.rpg = G <= R ? 1 : (int)((G + R - 1) / R);
+        }
+        v.push_back(p);
+        run *= (uint64_t)p.fan;
+    }
+    return v;
+}
+
+inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
+    return (sort_n == 0 || sort_n >= n) ? n : sort_n;
+}
+
+// Device scratch (bytes) one sort needs: binary splits or k-way range bounds,
+// plus an error word.
+template <class T>
+uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan) {
+    uint64_t bytes = merge_split_slots<T>(n) * sizeof(int64_t);
+    for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), fan)) {
+        if (p.fan > 2 && p.rpg > 1) {
+            const uint64_t b = p.groups * (uint64_t)(p.rpg + 1) * KWAY_MAX * sizeof(int64_t);
+            bytes = b > bytes ? b : bytes;
+        }
+    }
+    return bytes + 256;
+}
+
+// Sorts d[0..n) in chunks of sort_n (0 = one full sort) into `want` (d or
+// tmp). `key_mask` is XORed into every key on the way in and on the way out.
+// `scratch` holds pipeline_scratch_bytes<T>(n, sort_n, fan) bytes of device memory.
 template <class T>
 cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, T* want,
-                          int64_t* splits, cudaStream_t st, LaunchStats* stats) {
+                          int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
     using C = Config<T>;
+    using KC = KwayCfg<T>;
     constexpr int T1 = k1_tile<T>();
     constexpr int MT = merge_tile<T>();
     if (n == 0) return cudaSuccess;
     const bool full = (sort_n == 0 || sort_n >= n);
-    const uint64_t limit = full ? n : sort_n;
-    const int passes = limit > (uint64_t)T1 ? merge_passes(limit, T1) : 0;
+    const uint64_t limit = chunk_limit(n, sort_n);
+    const std::vector<PassPlan> plan = plan_passes<T>(n, limit, fan);
+    const int passes = (int)plan.size();
     const int k1_chunk = (int)(limit < (uint64_t)T1 ? (full ? T1 : limit) : T1);
     // the last writer must target `want`: with an even number of merge passes
     // K1 writes there itself (in place when want == d)
     T* other = (want == d) ? tmp : d;
     T* cur = (passes % 2 == 0) ? want : other;
+    int64_t* splits = static_cast<int64_t*>(scratch);
+    int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
+                                      pipeline_scratch_bytes<T>(n, sort_n, fan) - 256);
 
     static bool configured = false;
     if (!configured) {
@@ -95,12 +160,16 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         cudaFuncSetAttribute(pair_merge_kernel<T, C::M_NT, C::M_VT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
+        cudaFuncSetAttribute(range_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)KwayLayout<T>::SMEM);
         configured = true;
     }
 
     static const std::string n_k1 = std::string("block_sort<") + TypeName<T>::v + ">";
     static const std::string n_k4 = std::string("pair_partition<") + TypeName<T>::v + ">";
     static const std::string n_k3 = std::string("pair_merge<") + TypeName<T>::v + ">";
+    static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
+    static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
     launch(n_k1.c_str(), st, [&] {
         block_sort_kernel<T, C::K1_NT, C::K1_VT, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
@@ -110,24 +179,38 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
         stats->kernels++;
         stats->passes++;
     }
-    uint64_t run = T1;
-    for (int p = 0; p < passes; ++p) {
+    for (int pi = 0; pi < passes; ++pi) {
+        const PassPlan& p = plan[pi];
         T* nxt = (cur == want) ? other : want;
-        const uint64_t tiles = (n + MT - 1) / MT;
-        const unsigned pblocks = (unsigned)((tiles + 1 + 255) / 256);
-        launch(n_k4.c_str(), st, [&] {
-            pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
-        });
-        launch(n_k3.c_str(), st, [&] {
-            pair_merge_kernel<T, C::M_NT, C::M_VT><<<(unsigned)tiles, C::M_NT, merge_smem<T>(), st>>>(
-                cur, nxt, n, run, splits, p + 1 == passes ? key_mask : 0);
-        });
-        if (stats) {
-            stats->kernels += 2;
-            stats->passes++;
+        const uint64_t xo = pi + 1 == passes ? key_mask : 0;
+        if (p.fan == 2) {
+            const uint64_t tiles = (n + MT - 1) / MT;
+            const unsigned pblocks = (unsigned)((tiles + 1 + 255) / 256);
+            const uint64_t run = p.run;
+            launch(n_k4.c_str(), st, [&] {
+                pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
+            });
+            launch(n_k3.c_str(), st, [&] {
+                pair_merge_kernel<T, C::M_NT, C::M_VT><<<(unsigned)tiles, C::M_NT, merge_smem<T>(), st>>>(
+                    cur, nxt, n, run, splits, xo);
+            });
+            if (stats) stats->kernels += 2;
+        } else {
+            if (p.rpg > 1) {
+                launch(n_ks.c_str(), st, [&] {
+                    kway_split_kernel<T><<<(unsigned)(p.groups * (p.rpg + 1)), 256, 0, st>>>(
+                        cur, n, p.run, p.fan, p.rpg, splits, err);
+                });
+                if (stats) stats->kernels++;
+            }
+            launch(n_km.c_str(), st, [&] {
+                range_merge_kernel<T><<<(unsigned)(p.groups * p.rpg), KC::NT, KwayLayout<T>::SMEM, st>>>(
+                    cur, nxt, n, p.run, p.fan, p.rpg, p.rpg > 1 ? splits : nullptr, xo);
+            });
+            if (stats) stats->kernels++;
         }
+        if (stats) stats->passes++;
         cur = nxt;
-        run <<= 1;
     }
     return cudaGetLastError();
 }

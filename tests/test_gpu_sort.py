@@ -83,18 +83,15 @@ def expected(a, sort_n=0):
     """Stable chunk sort (numpy) - equal to the GPU output bit for bit."""
     n = len(a)
     step = n if sort_n == 0 or sort_n >= n else sort_n
-    out = np.empty_like(a)
     keys = orc.keys_of(a)
-    for c in range(0, n, max(step, 1)):
-        idx = np.argsort(keys[c:c + step], kind="stable")
-        out[c:c + step] = a[c:c + step][idx]
-    return out
+    chunk = np.arange(n, dtype=np.int64) // max(step, 1)
+    return a[np.lexsort((keys, chunk))]  # lexsort is stable
 
 
-def gpu_sort_device(a, kind, sort_n=0, result_in_tmp=False):
+def gpu_sort_device(a, kind, sort_n=0, result_in_tmp=False, min_k=0):
     d = to_dev(a)
     t = torch.empty_like(d)
-    r = og.sort(d, t, sort_n=sort_n, kind=kind, result_in_tmp=result_in_tmp)
+    r = og.sort(d, t, sort_n=sort_n, min_k=min_k, kind=kind, result_in_tmp=result_in_tmp)
     assert (r is t) == result_in_tmp or len(a) == 0
     return to_host(r, a.dtype)
 
@@ -110,23 +107,42 @@ def check_against_oracle(kind, a, got, sort_n=0):
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [1, 2, 3, 31, 1000, 2047, 2048, 2049, 4096, 8191, 8192, 8193,
                                65541, 300007])
-def test_sizes(kind, n):
+@pytest.mark.parametrize("min_k", [2, 4, 0])
+def test_sizes(kind, n, min_k):
     a = make(kind, n, "uniform")
-    check_against_oracle(kind, a, gpu_sort_device(a, kind))
+    check_against_oracle(kind, a, gpu_sort_device(a, kind, min_k=min_k))
+
+
+DISTS = ["uniform", "equal", "sorted", "reverse", "few", "zipf", "runs8"]
 
 
 @pytest.mark.parametrize("kind", KINDS)
-@pytest.mark.parametrize("dist", ["uniform", "equal", "sorted", "reverse", "few", "zipf", "runs8"])
-def test_distributions(kind, dist):
+@pytest.mark.parametrize("dist", DISTS)
+@pytest.mark.parametrize("min_k", [2, 16])
+def test_distributions(kind, dist, min_k):
     a = make(kind, (1 << 18) + 3, dist, seed=1)
-    check_against_oracle(kind, a, gpu_sort_device(a, kind))
+    check_against_oracle(kind, a, gpu_sort_device(a, kind, min_k=min_k))
+
+
+# sizes at which a k-way pass splits its groups into exact ranges (K4)
+RANGED = {og.U32: 3 * (1 << 20) + 7, og.U64: 3 * (1 << 19) + 5, og.I64: 3 * (1 << 19) + 5,
+          og.KV64: 600_001, og.KVU64: 600_001}
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("dist", DISTS)
+@pytest.mark.parametrize("min_k", [4, 8, 16])
+def test_kway_ranges(kind, dist, min_k):
+    a = make(kind, RANGED[kind], dist, seed=7)
+    check_against_oracle(kind, a, gpu_sort_device(a, kind, min_k=min_k))
 
 
 @pytest.mark.parametrize("kind", [og.U32, og.I64, og.KV64])
-@pytest.mark.parametrize("sort_n", [2, 8, 64, 1024, 2048, 4096, 8192, 65536])
-def test_chunked(kind, sort_n):
-    a = make(kind, (1 << 18) + 1000, "uniform", seed=2)
-    check_against_oracle(kind, a, gpu_sort_device(a, kind, sort_n), sort_n)
+@pytest.mark.parametrize("sort_n", [2, 8, 64, 1024, 2048, 4096, 8192, 65536, 1 << 20])
+@pytest.mark.parametrize("min_k", [2, 0])
+def test_chunked(kind, sort_n, min_k):
+    a = make(kind, (1 << 21) + 1000, "uniform", seed=2)
+    check_against_oracle(kind, a, gpu_sort_device(a, kind, sort_n, min_k=min_k), sort_n)
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -199,7 +215,8 @@ def test_merge_series(kind, merge_start, sort_n):
     assert np.array_equal(to_host(r, a.dtype), expected(runs, sort_n))
 
 
-@pytest.mark.parametrize("kind,n", [(og.U32, 1 << 26), (og.U64, 1 << 25), (og.KV64, 1 << 24)])
+@pytest.mark.parametrize("kind,n", [(og.U32, 1 << 26), (og.U64, 1 << 25), (og.KV64, 1 << 24),
+                                    (og.U32, (1 << 28) + 12345)])
 def test_large_against_torch_sort(kind, n):
     g = torch.Generator(device="cuda").manual_seed(11)
     words = 4 if kind == og.U32 else (8 if kind == og.U64 else 16)
