@@ -197,6 +197,10 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
                      int flags, void** result, cudaStream_t st) {
     const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
     if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
+    // device kernels move whole items with vector loads and cp.async
+    const unsigned ib = item_bytes(kind);
+    if (((uintptr_t)d % ib) || (tmp && ((uintptr_t)tmp % ib)))
+        return fail(ORIGAMI_ERR_ALIGN, "device buffers must be %u-byte aligned", ib);
     *result = in_tmp ? tmp : d;
     if (n <= 1) {
         if (n == 1 && in_tmp)

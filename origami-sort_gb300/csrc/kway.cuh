@@ -39,23 +39,28 @@ __device__ __forceinline__ bool less(const SampleE<K>& a, const SampleE<K>& b) {
 // Merge `nl` (a power of two <= 16) sorted lists held back to back in padded
 // shared memory (list i = src[off[i] .. off[i+1]), off[nl] == tot) into one list.
 // Each round merges adjacent pairs by merge path; the lower-indexed list wins
-// ties in every round, so the result is ordered by (key, list index). `off` is
-// rewritten. Returns the buffer holding the result (src or dst). Must be called
-// by all NT threads of the block.
+// ties in every round, so the result is ordered by (key, list index). Round r
+// sees the lists of the previous round, whose boundaries are off[k << r].
+// Returns the buffer holding the result (src or dst). All NT threads call it.
 template <class E, int NT, int VT>
-__device__ E* smem_merge_lists(E* src, E* dst, int* off, int nl, int tot) {
+__device__ E* smem_merge_lists(E* src, E* dst, const int* off, int nl, int tot) {
     const int tid = threadIdx.x;
-    while (nl > 1) {
-        const int npairs = nl >> 1;
+    for (int r = 0; (nl >> r) > 1; ++r) {
+        const int npairs = nl >> (r + 1);
+        int ps[KWAY_MAX / 2];
+#pragma unroll
+        for (int q = 0; q < KWAY_MAX / 2; ++q) ps[q] = (q < npairs) ? off[(2 * q) << r] : tot;
         for (int k0 = tid * VT; k0 < tot; k0 += NT * VT) {
             int k = k0;
             const int kend = min(k0 + VT, tot);
             while (k < kend) {
                 // the pair holding output k: the last pair starting at or before k
                 int p = 0;
-                for (int q = 1; q < npairs; ++q)
-                    if (off[2 * q] <= k) p = q;
-                const int a0 = off[2 * p], b0 = off[2 * p + 1], e0 = off[2 * p + 2];
+#pragma unroll
+                for (int q = 1; q < KWAY_MAX / 2; ++q)
+                    if (q < npairs && ps[q] <= k) p = q;
+                const int a0 = off[(2 * p) << r], b0 = off[(2 * p + 1) << r];
+                const int e0 = off[(2 * p + 2) << r];
                 const int diag = k - a0;
                 const int a = smem_merge_path(src, a0, b0 - a0, b0, e0 - b0, diag);
                 const int cnt = min(kend, e0) - k;
@@ -77,15 +82,26 @@ __device__ E* smem_merge_lists(E* src, E* dst, int* off, int nl, int tot) {
             }
         }
         __syncthreads();
-        if (tid == 0)
-            for (int q = 0; q <= npairs; ++q) off[q] = off[2 * q];
-        __syncthreads();
         E* t = src;
         src = dst;
         dst = t;
-        nl = npairs;
     }
     return src;
+}
+
+// Asynchronous global -> shared copy of one item (cp.async; no register staging).
+template <class T>
+__device__ __forceinline__ void cp_async_item(T* smem, const T* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
 // ------------------------------------------------------- K4: ranges ------
@@ -199,24 +215,31 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ s
 }
 
 // ------------------------------------------------------- K3: ranges ------
+// Per item type: threads, items per thread per merge round, sample stride S,
+// tile capacity TMAX (tiles hold at most (M + F) * S <= TMAX items, nominal
+// M * S) and the exact range size RANGE produced by K4.
 template <class T>
 struct KwayCfg;
 template <>
 struct KwayCfg<uint32_t> {
-    static constexpr int NT = 512, VT = 16, S = 64, TMAX = 9216;
-    static constexpr int RANGE = 1 << 18;
-};
-template <>
-struct KwayCfg<uint64_t> {
-    static constexpr int NT = 512, VT = 8, S = 64, TMAX = 5120;
+    static constexpr int NT = 512, VT = 16, S = 32, TMAX = 6656;
     static constexpr int RANGE = 1 << 17;
 };
 template <>
-struct KwayCfg<KV64> {
-    static constexpr int NT = 256, VT = 8, S = 32, TMAX = 2560;
+struct KwayCfg<uint64_t> {
+    static constexpr int NT = 512, VT = 8, S = 32, TMAX = 3584;
     static constexpr int RANGE = 1 << 16;
 };
+template <>
+struct KwayCfg<KV64> {
+    static constexpr int NT = 256, VT = 8, S = 16, TMAX = 1792;
+    static constexpr int RANGE = 1 << 15;
+};
 
+// Shared memory: three tile buffers (two inputs - the tile being merged and the
+// next one arriving by cp.async - and one merge scratch), then the per-range
+// tables. While the range's samples are merged the three buffers are used as two
+// halves for the sample ping-pong.
 template <class T>
 struct KwayLayout {
     using C = KwayCfg<T>;
@@ -224,11 +247,14 @@ struct KwayLayout {
     using E = SampleE<K>;
     static constexpr int CAP_ITEMS = padded_items<T>(C::TMAX + 1);  // per buffer
     static constexpr size_t BUF_BYTES = ((size_t)CAP_ITEMS * sizeof(T) + 15) & ~(size_t)15;
-    static constexpr int SCAP = (int)(BUF_BYTES / sizeof(E)) - (int)(BUF_BYTES / sizeof(E)) / pad_stride<E>() - 2;
+    static constexpr size_t SBUF_BYTES = (3 * BUF_BYTES / 2) & ~(size_t)15;
+    static constexpr int SCAP = (int)(SBUF_BYTES / sizeof(E)) - (int)(SBUF_BYTES / sizeof(E)) / pad_stride<E>() - 2;
     static constexpr int M = C::TMAX / C::S - KWAY_MAX;  // merged samples per tile
     static constexpr int MAXTILES = C::RANGE / (M * C::S) + 2;
-    static constexpr size_t SMEM = 2 * BUF_BYTES + (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + 256;
-    static_assert(C::RANGE / C::S <= SCAP, "range samples must fit one buffer");
+    static constexpr size_t TAB_BYTES = (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + (size_t)(MAXTILES + 1) * (KWAY_MAX + 1) * 4;
+    static constexpr size_t SMEM = 3 * BUF_BYTES + TAB_BYTES + 64;
+    static_assert(C::RANGE / C::S <= SCAP, "range samples must fit the sample buffers");
+    static_assert(C::NT * C::VT >= C::TMAX, "one merge round covers a whole tile");
 };
 
 // One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
@@ -242,15 +268,14 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     using E = SampleE<K>;
     constexpr int NT = C::NT, VT = C::VT, S = C::S, M = Lay::M;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* bufA = reinterpret_cast<T*>(smem_raw);
-    T* bufB = reinterpret_cast<T*>(smem_raw + Lay::BUF_BYTES);
-    uint32_t* sp = reinterpret_cast<uint32_t*>(smem_raw + 2 * Lay::BUF_BYTES);  // [MAXTILES+1][16]
-    uint32_t* hist = sp + (Lay::MAXTILES + 1) * KWAY_MAX;                      // [MAXTILES+1][16]
+    auto buf = [&](int i) { return reinterpret_cast<T*>(smem_raw + (size_t)i * Lay::BUF_BYTES); };
+    uint32_t* sp = reinterpret_cast<uint32_t*>(smem_raw + 3 * Lay::BUF_BYTES);  // [MAXTILES+1][16]
+    uint32_t* hist = sp + (Lay::MAXTILES + 1) * KWAY_MAX;                       // [MAXTILES+1][16]
+    int* toff = reinterpret_cast<int*>(hist + (Lay::MAXTILES + 1) * KWAY_MAX);  // [MAXTILES+1][17]
     __shared__ int off[KWAY_MAX + 1];
     __shared__ int64_t lo[KWAY_MAX];
     __shared__ uint32_t len[KWAY_MAX];
     __shared__ uint64_t out_base;
-    __shared__ int ntiles;
     const int tid = threadIdx.x;
 
     // --- range geometry
@@ -285,30 +310,30 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     const int nl = (geo.nr <= 1) ? 1 : (geo.nr <= 2 ? 2 : (geo.nr <= 4 ? 4 : (geo.nr <= 8 ? 8 : 16)));
 
     // --- fine samples: the last item of every full S-block of every run
-    E* sA = reinterpret_cast<E*>(bufA);
-    E* sB = reinterpret_cast<E*>(bufB);
+    E* sA = reinterpret_cast<E*>(smem_raw);
+    E* sB = reinterpret_cast<E*>(smem_raw + Lay::SBUF_BYTES);
     for (int q = 0; q < geo.nr; ++q) {
         const int c = off[q + 1] - off[q];
         const T* rp = src + lo[q];
+        const int o0 = off[q];
         for (int k = tid; k < c; k += NT) {
             E e;
             e.key = Traits<T>::key(rp[(uint64_t)(k + 1) * S - 1]);
             e.tag = ((uint32_t)k << 4) | (uint32_t)q;
-            sA[pad<E>(off[q] + k)] = e;
+            sA[pad<E>(o0 + k)] = e;
         }
     }
-    // runs beyond nr hold no samples, so off[nr..16] == nsamp already
-    __syncthreads();
+    __syncthreads();  // runs beyond nr hold no samples, so off[nr..16] == nsamp
     E* merged = sA;
     if (nl > 1 && nsamp > 0) merged = smem_merge_lists<E, NT, VT>(sA, sB, off, nl, nsamp);
 
     // --- tile cuts at merged samples M-1, 2M-1, ...
     const int nt = nsamp / M + 1;
-    for (int q = tid; q < nt * KWAY_MAX; q += NT) hist[q] = 0;
+    for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) hist[q] = 0;
     __syncthreads();
     for (int q = tid; q < nsamp; q += NT) atomicAdd(&hist[(q / M) * KWAY_MAX + (merged[pad<E>(q)].tag & 15)], 1u);
     __syncthreads();
-    // prefix over tiles: P[b][j] = samples of run j at merged positions < b*M
+    // exclusive prefix over tiles: hist[b][j] = run-j samples at merged positions < b*M
     if (tid < KWAY_MAX) {
         uint32_t acc = 0;
         for (int b = 0; b < nt; ++b) {
@@ -319,7 +344,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         hist[nt * KWAY_MAX + tid] = acc;
     }
     __syncthreads();
-    // splits: sp[b][j] = items of run j (relative to lo[j]) at or before cut b
+    // sp[b][j] = items of run j (relative to lo[j]) that precede cut b
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) {
         const int b = q / KWAY_MAX, j = q % KWAY_MAX;
         uint32_t v;
@@ -330,14 +355,14 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         } else {
             const E gs = merged[pad<E>(b * M - 1)];
             const int gi = (int)(gs.tag & 15);
-            const uint32_t pj = hist[b * KWAY_MAX + j];  // run-j samples at positions <= b*M-1
+            const uint32_t pj = hist[b * KWAY_MAX + j];
             if (j == gi) {
                 v = pj * S;
             } else {
                 uint32_t a = pj * S;
                 uint32_t e = min(a + (uint32_t)(S - 1), len[j]);
                 const T* rp = src + lo[j];
-                const bool le = j < gi;
+                const bool le = j < gi;  // earlier runs precede on equal keys
                 while (a < e) {
                     const uint32_t mid = (a + e) >> 1;
                     const K kv = Traits<T>::key(rp[mid]);
@@ -351,36 +376,51 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         }
         sp[q] = v;
     }
-    if (tid == 0) ntiles = nt;
+    __syncthreads();
+    // per-tile list offsets: toff[t][q] = items of tile t taken from runs < q
+    for (int t = tid; t < nt; t += NT) {
+        int o = 0;
+        for (int q = 0; q < KWAY_MAX; ++q) {
+            toff[t * (KWAY_MAX + 1) + q] = o;
+            o += (int)(sp[(t + 1) * KWAY_MAX + q] - sp[t * KWAY_MAX + q]);
+        }
+        toff[t * (KWAY_MAX + 1) + KWAY_MAX] = o;
+    }
     __syncthreads();
 
-    // --- tiles
-    for (int t = 0; t < ntiles; ++t) {
-        if (tid == 0) {
-            int o = 0;
-            for (int q = 0; q < KWAY_MAX; ++q) {
-                off[q] = o;
-                o += (int)(sp[(t + 1) * KWAY_MAX + q] - sp[t * KWAY_MAX + q]);
-            }
-            off[KWAY_MAX] = o;
-        }
-        __syncthreads();
-        const int tot = off[KWAY_MAX];
+    // --- tiles: cp.async prefetch of tile t+1 overlaps the merge of tile t
+    auto issue = [&](int t, T* b) {
+        const int* to = toff + t * (KWAY_MAX + 1);
         for (int q = 0; q < geo.nr; ++q) {
-            const int l = off[q + 1] - off[q];
+            const int o0 = to[q];
+            const int l = to[q + 1] - o0;
             const T* rp = src + lo[q] + sp[t * KWAY_MAX + q];
-            const int o0 = off[q];
-            for (int k = tid; k < l; k += NT) bufA[pad<T>(o0 + k)] = rp[k];
+            for (int k = tid; k < l; k += NT) cp_async_item(&b[pad<T>(o0 + k)], rp + k);
         }
+        cp_async_commit();
+    };
+    issue(0, buf(0));
+    int cur = 0;
+    for (int t = 0; t < nt; ++t) {
+        const int nxt = cur == 0 ? 1 : 0;
+        if (t + 1 < nt)
+            issue(t + 1, buf(nxt));
+        else
+            cp_async_commit();
+        cp_async_wait<1>();
         __syncthreads();
-        T* res = bufA;
-        if (nl > 1) res = smem_merge_lists<T, NT, VT>(bufA, bufB, off, nl, tot);
+        const int* to = toff + t * (KWAY_MAX + 1);
+        const int tot = to[KWAY_MAX];
+        T* res = buf(cur);
+        if (nl > 1) res = smem_merge_lists<T, NT, VT>(buf(cur), buf(2), to, nl, tot);
         uint64_t ob = out_base;
         for (int q = 0; q < KWAY_MAX; ++q) ob += sp[t * KWAY_MAX + q];
         T* op = dst + ob;
         for (int k = tid; k < tot; k += NT) op[k] = Traits<T>::flip(res[pad<T>(k)], xout);
         __syncthreads();
+        cur = nxt;
     }
+    cp_async_wait<0>();
 }
 
 }  // namespace origami
