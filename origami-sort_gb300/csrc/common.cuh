@@ -24,6 +24,7 @@ struct Traits;
 template <>
 struct Traits<uint32_t> {
     using Key = uint32_t;
+    static constexpr bool kStable = false;  // keys only: equal items are identical
     static __host__ __device__ __forceinline__ Key key(uint32_t v) { return v; }
     static __device__ __forceinline__ uint32_t flip(uint32_t v, uint64_t x) { return v ^ (uint32_t)x; }
     static __device__ __forceinline__ uint32_t max_item() { return 0xFFFFFFFFu; }
@@ -32,6 +33,7 @@ struct Traits<uint32_t> {
 template <>
 struct Traits<uint64_t> {
     using Key = uint64_t;
+    static constexpr bool kStable = false;
     static __host__ __device__ __forceinline__ Key key(uint64_t v) { return v; }
     static __device__ __forceinline__ uint64_t flip(uint64_t v, uint64_t x) { return v ^ x; }
     static __device__ __forceinline__ uint64_t max_item() { return ~0ull; }
@@ -40,6 +42,7 @@ struct Traits<uint64_t> {
 template <>
 struct Traits<KV64> {
     using Key = uint64_t;
+    static constexpr bool kStable = true;  // values must keep their input order
     static __host__ __device__ __forceinline__ Key key(const KV64& v) { return v.key; }
     static __device__ __forceinline__ KV64 flip(KV64 v, uint64_t x) {
         v.key ^= x;

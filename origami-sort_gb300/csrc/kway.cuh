@@ -20,6 +20,7 @@
 // stable across runs and gives every item exactly one place.
 #pragma once
 #include "common.cuh"
+#include "merge_core.cuh"
 
 namespace origami {
 
@@ -253,6 +254,7 @@ struct KwayLayout {
     static constexpr int MAXTILES = C::RANGE / (M * C::S) + 2;
     static constexpr size_t TAB_BYTES = (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + (size_t)(MAXTILES + 1) * (KWAY_MAX + 1) * 4;
     static constexpr size_t SMEM = 3 * BUF_BYTES + TAB_BYTES + 64;
+    static constexpr int MAXBLK = (C::TMAX > C::RANGE / C::S ? C::TMAX : C::RANGE / C::S) / C::VT + KWAY_MAX;
     static_assert(C::RANGE / C::S <= SCAP, "range samples must fit the sample buffers");
     static_assert(C::NT * C::VT >= C::TMAX, "one merge round covers a whole tile");
 };
@@ -273,6 +275,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     uint32_t* hist = sp + (Lay::MAXTILES + 1) * KWAY_MAX;                       // [MAXTILES+1][16]
     int* toff = reinterpret_cast<int*>(hist + (Lay::MAXTILES + 1) * KWAY_MAX);  // [MAXTILES+1][17]
     __shared__ int off[KWAY_MAX + 1];
+    __shared__ int mblk[Lay::MAXBLK];  // merge-round block splits
     __shared__ int64_t lo[KWAY_MAX];
     __shared__ uint32_t len[KWAY_MAX];
     __shared__ uint64_t out_base;
@@ -325,7 +328,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     }
     __syncthreads();  // runs beyond nr hold no samples, so off[nr..16] == nsamp
     E* merged = sA;
-    if (nl > 1 && nsamp > 0) merged = smem_merge_lists<E, NT, VT>(sA, sB, off, nl, nsamp);
+    if (nl > 1 && nsamp > 0) merged = merge_lists<E, NT, VT, KWAY_MAX / 2, true>(sA, sB, off, nl, mblk);
 
     // --- tile cuts at merged samples M-1, 2M-1, ...
     const int nt = nsamp / M + 1;
@@ -412,7 +415,8 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         const int* to = toff + t * (KWAY_MAX + 1);
         const int tot = to[KWAY_MAX];
         T* res = buf(cur);
-        if (nl > 1) res = smem_merge_lists<T, NT, VT>(buf(cur), buf(2), to, nl, tot);
+        if (nl > 1)
+            res = merge_lists<T, NT, VT, KWAY_MAX / 2, Traits<T>::kStable>(buf(cur), buf(2), to, nl, mblk);
         uint64_t ob = out_base;
         for (int q = 0; q < KWAY_MAX; ++q) ob += sp[t * KWAY_MAX + q];
         T* op = dst + ob;

@@ -22,13 +22,13 @@ struct Config;
 // that a merge tile never straddles two run pairs.
 template <>
 struct Config<uint32_t> {
-    static constexpr int K1_NT = 512, K1_VT = 16;  // 8192-item tiles (32 KiB)
+    static constexpr int K1_NT = 256, K1_VT = 32;  // 8192-item tiles (32 KiB)
     static constexpr int M_NT = 256, M_VT = 16;    // 4096-item merge tiles
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<uint64_t> {
-    static constexpr int K1_NT = 512, K1_VT = 8;  // 4096 items (32 KiB)
+    static constexpr int K1_NT = 256, K1_VT = 16;  // 4096 items (32 KiB)
     static constexpr int M_NT = 256, M_VT = 8;    // 2048
     static constexpr bool STABLE = false;
 };
@@ -48,8 +48,8 @@ constexpr int merge_tile() {
     return Config<T>::M_NT * Config<T>::M_VT;
 }
 template <class T>
-constexpr size_t k1_smem() {
-    return (size_t)padded_items<T>(k1_tile<T>() + Config<T>::K1_VT) * sizeof(T);
+constexpr size_t k1_smem() {  // two padded tile buffers (merge rounds ping-pong)
+    return 2 * (size_t)padded_items<T>(k1_tile<T>() + Config<T>::K1_VT) * sizeof(T);
 }
 template <class T>
 constexpr size_t merge_smem() {

@@ -6,13 +6,16 @@
 //                               shared memory and merged by merge path
 #pragma once
 #include "common.cuh"
+#include "merge_core.cuh"
 
 namespace origami {
 
 // ---------------------------------------------------------------- K1 -----
 // Sorts tiles of NT*VT items. Restates the reference's phase 1 + phase 2
 // (sorter.h:3831-3849: in-register networks, then binary merges up to the
-// in-cache block size) with the tile held in registers and shared memory.
+// in-cache block size): each thread sorts VT items in registers, then
+// log2(NT) merge rounds in shared memory (merge_core.cuh) double the run length
+// until the tile (or the chunk) is sorted.
 // `chunk` (power of two) caps the sorted run length for chunked sorts.
 // xin/xout are the key masks applied on load / on store (sign flip for i64).
 template <class T, int NT, int VT, bool STABLE>
@@ -20,8 +23,11 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
                                                         uint64_t n, int chunk, uint64_t xin,
                                                         uint64_t xout) {
     constexpr int TILE = NT * VT;
+    constexpr int BUF = padded_items<T>(TILE + VT);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s = reinterpret_cast<T*>(smem_raw);
+    T* sa = reinterpret_cast<T*>(smem_raw);
+    T* sb = sa + BUF;
+    __shared__ int split[TILE / VT + 1];
     const int tid = threadIdx.x;
     const uint64_t base = (uint64_t)blockIdx.x * TILE;
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
@@ -31,33 +37,31 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
 #pragma unroll
     for (int k = 0; k < VT; ++k) {
         const int i = k * NT + tid;
-        s[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
+        sa[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
     }
     __syncthreads();
-    T v[VT];
+    {
+        T v[VT];
 #pragma unroll
-    for (int k = 0; k < VT; ++k) v[k] = s[pad<T>(tid * VT + k)];
-    thread_sort<T, VT, STABLE>(v, chunk);
-
+        for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(tid * VT + k)];
+        thread_sort<T, VT, STABLE>(v, chunk);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < VT; ++k) sa[pad<T>(tid * VT + k)] = v[k];
+    }
+    __syncthreads();
+    T* src = sa;
+    T* dst = sb;
     for (int w = VT; w < TILE && w < chunk; w <<= 1) {
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < VT; ++k) s[pad<T>(tid * VT + k)] = v[k];
-        __syncthreads();
-        const int o = tid * VT;
-        const int b0 = o & ~(2 * w - 1);
-        const int diag = o - b0;
-        const int a = smem_merge_path(s, b0, w, b0 + w, w, diag);
-        smem_serial_merge<T, VT>(s, b0 + a, b0 + w, b0 + w + diag - a, b0 + 2 * w, v);
+        merge_round_uniform<T, NT, VT, STABLE>(src, dst, w, TILE, split);
+        T* t = src;
+        src = dst;
+        dst = t;
     }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < VT; ++k) s[pad<T>(tid * VT + k)] = v[k];
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < VT; ++k) {
         const int i = k * NT + tid;
-        if (i < valid) out[base + i] = Traits<T>::flip(s[pad<T>(i)], xout);
+        if (i < valid) out[base + i] = Traits<T>::flip(src[pad<T>(i)], xout);
     }
 }
 
