@@ -37,59 +37,6 @@ __device__ __forceinline__ bool less(const SampleE<K>& a, const SampleE<K>& b) {
     return a.key < b.key;
 }
 
-// Merge `nl` (a power of two <= 16) sorted lists held back to back in padded
-// shared memory (list i = src[off[i] .. off[i+1]), off[nl] == tot) into one list.
-// Each round merges adjacent pairs by merge path; the lower-indexed list wins
-// ties in every round, so the result is ordered by (key, list index). Round r
-// sees the lists of the previous round, whose boundaries are off[k << r].
-// Returns the buffer holding the result (src or dst). All NT threads call it.
-template <class E, int NT, int VT>
-__device__ E* smem_merge_lists(E* src, E* dst, const int* off, int nl, int tot) {
-    const int tid = threadIdx.x;
-    for (int r = 0; (nl >> r) > 1; ++r) {
-        const int npairs = nl >> (r + 1);
-        int ps[KWAY_MAX / 2];
-#pragma unroll
-        for (int q = 0; q < KWAY_MAX / 2; ++q) ps[q] = (q < npairs) ? off[(2 * q) << r] : tot;
-        for (int k0 = tid * VT; k0 < tot; k0 += NT * VT) {
-            int k = k0;
-            const int kend = min(k0 + VT, tot);
-            while (k < kend) {
-                // the pair holding output k: the last pair starting at or before k
-                int p = 0;
-#pragma unroll
-                for (int q = 1; q < KWAY_MAX / 2; ++q)
-                    if (q < npairs && ps[q] <= k) p = q;
-                const int a0 = off[(2 * p) << r], b0 = off[(2 * p + 1) << r];
-                const int e0 = off[(2 * p + 2) << r];
-                const int diag = k - a0;
-                const int a = smem_merge_path(src, a0, b0 - a0, b0, e0 - b0, diag);
-                const int cnt = min(kend, e0) - k;
-                int ia = a0 + a, ib = b0 + diag - a;
-                E x = src[pad<E>(ia)];
-                E y = src[pad<E>(ib)];
-#pragma unroll
-                for (int i = 0; i < VT; ++i) {
-                    if (i < cnt) {
-                        const bool takeA = (ib >= e0) || (ia < b0 && !less(y, x));
-                        dst[pad<E>(k + i)] = takeA ? x : y;
-                        const int nxt = takeA ? ++ia : ++ib;
-                        const E v = src[pad<E>(nxt)];
-                        x = takeA ? v : x;
-                        y = takeA ? y : v;
-                    }
-                }
-                k += cnt;
-            }
-        }
-        __syncthreads();
-        E* t = src;
-        src = dst;
-        dst = t;
-    }
-    return src;
-}
-
 // Asynchronous global -> shared copy of one item (cp.async; no register staging).
 template <class T>
 __device__ __forceinline__ void cp_async_item(T* smem, const T* gmem) {
@@ -221,54 +168,69 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ s
 // M * S) and the exact range size RANGE produced by K4.
 template <class T>
 struct KwayCfg;
+// NT threads; VT registers per merge block (blocks of VT-1 outputs for keys,
+// VT for key-value); sample stride S; tile capacity TMAX (tiles hold at most
+// (M + 16) * S items, nominal M * S with M = TMAX / S - 16); exact range size
+// RANGE produced by K4.
 template <>
 struct KwayCfg<uint32_t> {
-    static constexpr int NT = 512, VT = 16, S = 32, TMAX = 6656;
+    static constexpr int NT = 256, VT = 32, S = 32, TMAX = 8704;
     static constexpr int RANGE = 1 << 17;
 };
 template <>
 struct KwayCfg<uint64_t> {
-    static constexpr int NT = 512, VT = 8, S = 32, TMAX = 3584;
+    static constexpr int NT = 256, VT = 16, S = 32, TMAX = 4096;
     static constexpr int RANGE = 1 << 16;
 };
 template <>
 struct KwayCfg<KV64> {
-    static constexpr int NT = 256, VT = 8, S = 16, TMAX = 1792;
+    static constexpr int NT = 256, VT = 7, S = 16, TMAX = 1792;
     static constexpr int RANGE = 1 << 15;
 };
 
-// Shared memory: three tile buffers (two inputs - the tile being merged and the
-// next one arriving by cp.async - and one merge scratch), then the per-range
-// tables. While the range's samples are merged the three buffers are used as two
-// halves for the sample ping-pong.
+// Shared memory: three unpadded tile buffers (the tile being merged, the next
+// one arriving by cp.async, and a merge scratch), then the per-range tables.
+// While the range's samples are merged the three buffers serve as two halves
+// of the sample ping-pong.
 template <class T>
 struct KwayLayout {
     using C = KwayCfg<T>;
     using K = typename Traits<T>::Key;
     using E = SampleE<K>;
-    static constexpr int CAP_ITEMS = padded_items<T>(C::TMAX + 1);  // per buffer
+    static constexpr int EVT = 7;  // sample merge: serial blocks of 7
+    static constexpr int CAP_ITEMS = C::TMAX + C::VT + 2;  // per buffer, with read slack
     static constexpr size_t BUF_BYTES = ((size_t)CAP_ITEMS * sizeof(T) + 15) & ~(size_t)15;
     static constexpr size_t SBUF_BYTES = (3 * BUF_BYTES / 2) & ~(size_t)15;
-    static constexpr int SCAP = (int)(SBUF_BYTES / sizeof(E)) - (int)(SBUF_BYTES / sizeof(E)) / pad_stride<E>() - 2;
+    static constexpr int SCAP = (int)(SBUF_BYTES / sizeof(E)) - EVT - 2;
     static constexpr int M = C::TMAX / C::S - KWAY_MAX;  // merged samples per tile
     static constexpr int MAXTILES = C::RANGE / (M * C::S) + 2;
-    static constexpr size_t TAB_BYTES = (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + (size_t)(MAXTILES + 1) * (KWAY_MAX + 1) * 4;
+    static constexpr size_t TAB_BYTES =
+        (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + (size_t)(MAXTILES + 1) * (KWAY_MAX + 1) * 4;
     static constexpr size_t SMEM = 3 * BUF_BYTES + TAB_BYTES + 64;
-    static constexpr int MAXBLK = (C::TMAX > C::RANGE / C::S ? C::TMAX : C::RANGE / C::S) / C::VT + KWAY_MAX;
+    static constexpr int VO = Block<T, C::VT, Traits<T>::kStable>::VO;
+    static constexpr int MAXBLK_T = C::TMAX / VO + KWAY_MAX + 2;
+    static constexpr int MAXBLK_S = (C::RANGE / C::S) / EVT + KWAY_MAX + 2;
+    static constexpr int MAXBLK = MAXBLK_T > MAXBLK_S ? MAXBLK_T : MAXBLK_S;
     static_assert(C::RANGE / C::S <= SCAP, "range samples must fit the sample buffers");
-    static_assert(C::NT * C::VT >= C::TMAX, "one merge round covers a whole tile");
+};
+
+// Phase hook of range_merge_kernel: the default does nothing and compiles away;
+// a measurement harness can pass a type that records clock64() per phase.
+struct NoProbe {
+    __device__ __forceinline__ void mark(int) {}
 };
 
 // One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
-template <class T>
+template <class T, class Probe = NoProbe>
 __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int F, int rpg,
-    const int64_t* __restrict__ bnd, uint64_t xout) {
+    const int64_t* __restrict__ bnd, uint64_t xout, Probe probe = Probe()) {
     using C = KwayCfg<T>;
     using Lay = KwayLayout<T>;
     using K = typename Traits<T>::Key;
     using E = SampleE<K>;
     constexpr int NT = C::NT, VT = C::VT, S = C::S, M = Lay::M;
+    (void)VT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto buf = [&](int i) { return reinterpret_cast<T*>(smem_raw + (size_t)i * Lay::BUF_BYTES); };
     uint32_t* sp = reinterpret_cast<uint32_t*>(smem_raw + 3 * Lay::BUF_BYTES);  // [MAXTILES+1][16]
@@ -312,6 +274,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     const int nsamp = off[KWAY_MAX];
     const int nl = (geo.nr <= 1) ? 1 : (geo.nr <= 2 ? 2 : (geo.nr <= 4 ? 4 : (geo.nr <= 8 ? 8 : 16)));
 
+    probe.mark(0);
     // --- fine samples: the last item of every full S-block of every run
     E* sA = reinterpret_cast<E*>(smem_raw);
     E* sB = reinterpret_cast<E*>(smem_raw + Lay::SBUF_BYTES);
@@ -323,18 +286,20 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
             E e;
             e.key = Traits<T>::key(rp[(uint64_t)(k + 1) * S - 1]);
             e.tag = ((uint32_t)k << 4) | (uint32_t)q;
-            sA[pad<E>(o0 + k)] = e;
+            sA[o0 + k] = e;
         }
     }
     __syncthreads();  // runs beyond nr hold no samples, so off[nr..16] == nsamp
+    probe.mark(1);
     E* merged = sA;
-    if (nl > 1 && nsamp > 0) merged = merge_lists<E, NT, VT, KWAY_MAX / 2, true>(sA, sB, off, nl, mblk);
+    if (nl > 1 && nsamp > 0) merged = merge_lists<E, NT, Lay::EVT, KWAY_MAX / 2, true>(sA, sB, off, nl, mblk);
 
+    probe.mark(2);
     // --- tile cuts at merged samples M-1, 2M-1, ...
     const int nt = nsamp / M + 1;
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) hist[q] = 0;
     __syncthreads();
-    for (int q = tid; q < nsamp; q += NT) atomicAdd(&hist[(q / M) * KWAY_MAX + (merged[pad<E>(q)].tag & 15)], 1u);
+    for (int q = tid; q < nsamp; q += NT) atomicAdd(&hist[(q / M) * KWAY_MAX + (merged[q].tag & 15)], 1u);
     __syncthreads();
     // exclusive prefix over tiles: hist[b][j] = run-j samples at merged positions < b*M
     if (tid < KWAY_MAX) {
@@ -347,6 +312,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         hist[nt * KWAY_MAX + tid] = acc;
     }
     __syncthreads();
+    probe.mark(3);
     // sp[b][j] = items of run j (relative to lo[j]) that precede cut b
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) {
         const int b = q / KWAY_MAX, j = q % KWAY_MAX;
@@ -356,7 +322,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         } else if (b == nt || j >= geo.nr) {
             v = (j < geo.nr) ? len[j] : 0;
         } else {
-            const E gs = merged[pad<E>(b * M - 1)];
+            const E gs = merged[b * M - 1];
             const int gi = (int)(gs.tag & 15);
             const uint32_t pj = hist[b * KWAY_MAX + j];
             if (j == gi) {
@@ -391,6 +357,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
     }
     __syncthreads();
 
+    probe.mark(4);
     // --- tiles: cp.async prefetch of tile t+1 overlaps the merge of tile t
     auto issue = [&](int t, T* b) {
         const int* to = toff + t * (KWAY_MAX + 1);
@@ -398,7 +365,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
             const int o0 = to[q];
             const int l = to[q + 1] - o0;
             const T* rp = src + lo[q] + sp[t * KWAY_MAX + q];
-            for (int k = tid; k < l; k += NT) cp_async_item(&b[pad<T>(o0 + k)], rp + k);
+            for (int k = tid; k < l; k += NT) cp_async_item(&b[o0 + k], rp + k);
         }
         cp_async_commit();
     };
@@ -410,18 +377,22 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
             issue(t + 1, buf(nxt));
         else
             cp_async_commit();
+        probe.mark(5);
         cp_async_wait<1>();
         __syncthreads();
+        probe.mark(6);
         const int* to = toff + t * (KWAY_MAX + 1);
         const int tot = to[KWAY_MAX];
         T* res = buf(cur);
         if (nl > 1)
             res = merge_lists<T, NT, VT, KWAY_MAX / 2, Traits<T>::kStable>(buf(cur), buf(2), to, nl, mblk);
+        probe.mark(7);
         uint64_t ob = out_base;
         for (int q = 0; q < KWAY_MAX; ++q) ob += sp[t * KWAY_MAX + q];
         T* op = dst + ob;
-        for (int k = tid; k < tot; k += NT) op[k] = Traits<T>::flip(res[pad<T>(k)], xout);
+        for (int k = tid; k < tot; k += NT) op[k] = Traits<T>::flip(res[k], xout);
         __syncthreads();
+        probe.mark(8);
         cur = nxt;
     }
     cp_async_wait<0>();

@@ -2,23 +2,37 @@
 // k-way tile merge (K3).
 //
 // A round merges adjacent pairs of sorted lists (A_p, B_p) from `src` into
-// `dst`, every pair writing its output over the positions it occupies. The
-// output of a pair is cut into blocks of VT items and one thread owns a block:
-// it finds where its block starts in A by merge path (Odeh et al.) and reads
-// where it ends from the next block's search, so its outputs are exactly the
-// merge of A[a0, a1) and B[b0, b1).
+// `dst`; every pair writes its output over the positions it occupies. A pair's
+// output is cut into blocks of VO items and one thread owns a block: it finds
+// where its block starts in A by merge path (Odeh et al.) and reads where it
+// ends from the next block's search, so its outputs are exactly the merge of
+// A[a0, a1) and B[b0, b1).
 //
-//  keys only  - the thread loads A[a0, a1) ascending and B[b0, b1) descending
-//               into VT registers (a bitonic sequence; a short block is filled
-//               with the largest key between the two parts) and sorts it with a
-//               bitonic half-cleaner network: VT/2*log2(VT) compare-exchanges,
-//               every load independent of the others;
-//  stable     - (key-value items) the thread merges serially, A first on equal
-//               keys, so equal keys keep their input order.
+//  keys only  - VO = VT - 1. The thread loads A[a0, a1) ascending, then the
+//               largest key, then B[b0, b1) descending into VT registers (a
+//               bitonic sequence) and sorts it with a bitonic half-cleaner
+//               network (VT/2*log2(VT) compare-exchanges); the loads are
+//               independent of each other.
+//  stable     - (key-value items) VO = VT. The thread merges serially, A first
+//               on equal keys, so equal keys keep their input order.
+//
+// Buffers are unpadded. VO is odd, so the blocks of the 32 threads of a warp
+// start 31 (or 7, 15) items apart and their stores fall on different banks.
+// A source may instead use the padded layout (one spare slot per 32 items),
+// which the tile sort uses once, for the blocked store after its register sort.
 #pragma once
 #include "common.cuh"
 
 namespace origami {
+
+// Index maps of a source buffer.
+struct LinIdx {
+    static __device__ __forceinline__ int at(int i) { return i; }
+};
+template <class T>
+struct PadIdx {
+    static __device__ __forceinline__ int at(int i) { return pad<T>(i); }
+};
 
 // Bitonic half-cleaner sort of a bitonic register sequence into ascending order.
 template <class T, int VT>
@@ -31,95 +45,123 @@ __device__ __forceinline__ void bitonic_clean(T (&v)[VT]) {
     }
 }
 
-// Merges one block: outputs [o, o + cnt) of the pair whose A part starts at
-// ia0 - sa, taking na = ea - sa items from A (starting at ia0) and the rest from
-// B (starting at ib0).
 template <class T, int VT, bool STABLE>
+struct Block {
+    static constexpr int VO = STABLE ? VT : VT - 1;  // outputs per block
+};
+
+// Merge path on a source with index map IX.
+template <class T, class IX>
+__device__ __forceinline__ int merge_path_ix(const T* s, int a0, int na, int b0, int nb, int diag) {
+    int lo = max(0, diag - nb);
+    int hi = min(diag, na);
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const T a = s[IX::at(a0 + mid)];
+        const T b = s[IX::at(b0 + diag - 1 - mid)];
+        if (!less(b, a))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Merges one block: cnt outputs at dst[o..], na of them from A starting at
+// src index ia0, the rest from B starting at ib0.
+template <class T, int VT, bool STABLE, class IX>
 __device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int ib0, int na, int cnt,
                                             int o) {
     const int nb = cnt - na;
     if constexpr (STABLE) {
         int ia = ia0, ib = ib0;
         const int aEnd = ia0 + na, bEnd = ib0 + nb;
-        T x = src[pad<T>(ia)];
-        T y = src[pad<T>(ib)];
+        T x = src[IX::at(ia)];
+        T y = src[IX::at(ib)];
 #pragma unroll
         for (int i = 0; i < VT; ++i) {
             if (i < cnt) {
                 const bool takeA = (ib >= bEnd) || (ia < aEnd && !less(y, x));
-                dst[pad<T>(o + i)] = takeA ? x : y;
+                dst[o + i] = takeA ? x : y;
                 const int nxt = takeA ? ++ia : ++ib;
-                const T vv = src[pad<T>(nxt)];
+                const T vv = src[IX::at(nxt)];
                 x = takeA ? vv : x;
                 y = takeA ? y : vv;
             }
         }
     } else {
         T v[VT];
+        const int pb = ib0 + VT - 1;  // B is read backwards: slot i holds B[pb - i]
 #pragma unroll
         for (int i = 0; i < VT; ++i) {
-            // [A ascending | largest key ... | B descending] is bitonic
             const bool fromA = i < na;
-            const bool fromB = (VT - 1 - i) < nb;
-            const int idx = fromA ? (ia0 + i) : (fromB ? ib0 + (VT - 1 - i) : ia0);
-            const T t = src[pad<T>(idx)];
-            v[i] = (fromA || fromB) ? t : Traits<T>::max_item();
+            const T t = src[IX::at(fromA ? ia0 + i : pb - i)];
+            // slots between the A part and the B part hold the largest key
+            v[i] = (fromA || i >= VT - nb) ? t : Traits<T>::max_item();
         }
         bitonic_clean<T, VT>(v);
+        if (cnt == VT - 1) {
 #pragma unroll
-        for (int i = 0; i < VT; ++i)
-            if (i < cnt) dst[pad<T>(o + i)] = v[i];
+            for (int i = 0; i < VT - 1; ++i) dst[o + i] = v[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < VT - 1; ++i)
+                if (i < cnt) dst[o + i] = v[i];
+        }
     }
 }
 
-// Round over pairs of equal width w (lists [2p*w, (2p+1)*w) and
-// [(2p+1)*w, (2p+2)*w) within `total` items; the last pair may be short or
-// absent). Used by the tile sort, where every list is a power-of-two run.
-// `split` is shared scratch of total/VT + 1 ints.
-template <class T, int NT, int VT, bool STABLE>
+// Round over pairs of equal width w inside `total` items (the last pair may be
+// short or absent): the tile sort's rounds. `split` is shared scratch of
+// blocks + 1 ints, blocks = ceil(total / VO) + total / (2w) + 1.
+template <class T, int NT, int VT, bool STABLE, class IX>
 __device__ __forceinline__ void merge_round_uniform(const T* src, T* dst, int w, int total, int* split) {
+    constexpr int VO = Block<T, VT, STABLE>::VO;
     const int tid = threadIdx.x;
-    const int nblk = (total + VT - 1) / VT;
+    const int bpp = (2 * w + VO - 1) / VO;  // blocks per full pair
+    const int npairs = (total + 2 * w - 1) / (2 * w);
+    const int nblk = npairs * bpp;
     for (int blk = tid; blk < nblk; blk += NT) {
-        const int o = blk * VT;
-        const int a0 = o & ~(2 * w - 1);
+        const int p = blk / bpp;
+        const int a0 = p * 2 * w;
         const int b0 = min(a0 + w, total), e0 = min(a0 + 2 * w, total);
-        split[blk] = smem_merge_path(src, a0, b0 - a0, b0, e0 - b0, o - a0);
+        const int diag = min((blk - p * bpp) * VO, e0 - a0);
+        split[blk] = merge_path_ix<T, IX>(src, a0, b0 - a0, b0, e0 - b0, diag);
     }
     __syncthreads();
     for (int blk = tid; blk < nblk; blk += NT) {
-        const int o = blk * VT;
-        const int a0 = o & ~(2 * w - 1);
+        const int p = blk / bpp;
+        const int a0 = p * 2 * w;
         const int b0 = min(a0 + w, total), e0 = min(a0 + 2 * w, total);
-        const int diag = o - a0;
-        const int cnt = min(VT, e0 - o);
+        const int diag = (blk - p * bpp) * VO;
+        const int cnt = min(VO, e0 - a0 - diag);
+        if (cnt <= 0) continue;
         const int sa = split[blk];
-        const int ea = (o + VT < e0) ? split[blk + 1] : (b0 - a0);
-        merge_block<T, VT, STABLE>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, o);
+        const int ea = (blk + 1 < (p + 1) * bpp) ? split[blk + 1] : (b0 - a0);
+        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag);
     }
     __syncthreads();
 }
 
 // Round over pairs of arbitrary lists: list i is [off[i*stride], off[(i+1)*stride])
-// and pair p = lists (2p, 2p+1), p < npairs <= MAXP. Blocks of VT outputs are
-// numbered pair by pair. `split` is shared scratch of total/VT + npairs + 1 ints.
-template <class T, int NT, int VT, int MAXP, bool STABLE>
+// and pair p = lists (2p, 2p+1), p < npairs <= MAXP. Blocks are numbered pair by
+// pair. `split` is shared scratch of total/VO + npairs + 1 ints.
+template <class T, int NT, int VT, int MAXP, bool STABLE, class IX>
 __device__ __forceinline__ void merge_round_lists(const T* src, T* dst, const int* off, int stride,
                                                   int npairs, int* split) {
+    constexpr int VO = Block<T, VT, STABLE>::VO;
     const int tid = threadIdx.x;
-    // bp[p] = first block of pair p (registers, unrolled)
-    int bp[MAXP + 1];
+    int bp[MAXP + 1];  // first block of each pair (registers, unrolled)
     {
         int acc = 0;
 #pragma unroll
         for (int p = 0; p < MAXP; ++p) {
             bp[p] = acc;
-            if (p < npairs) acc += (off[(2 * p + 2) * stride] - off[(2 * p) * stride] + VT - 1) / VT;
+            if (p < npairs) acc += (off[(2 * p + 2) * stride] - off[(2 * p) * stride] + VO - 1) / VO;
         }
         bp[MAXP] = acc;
     }
     const int nblk = bp[MAXP];
-    // pair of a block and the first block of that pair and of the next
     auto locate = [&](int blk, int& p, int& first, int& next) {
         p = 0;
         first = 0;
@@ -138,7 +180,7 @@ __device__ __forceinline__ void merge_round_lists(const T* src, T* dst, const in
         locate(blk, p, first, next);
         const int a0 = off[(2 * p) * stride], b0 = off[(2 * p + 1) * stride];
         const int e0 = off[(2 * p + 2) * stride];
-        split[blk] = smem_merge_path(src, a0, b0 - a0, b0, e0 - b0, (blk - first) * VT);
+        split[blk] = merge_path_ix<T, IX>(src, a0, b0 - a0, b0, e0 - b0, (blk - first) * VO);
     }
     __syncthreads();
     for (int blk = tid; blk < nblk; blk += NT) {
@@ -146,23 +188,24 @@ __device__ __forceinline__ void merge_round_lists(const T* src, T* dst, const in
         locate(blk, p, first, next);
         const int a0 = off[(2 * p) * stride], b0 = off[(2 * p + 1) * stride];
         const int e0 = off[(2 * p + 2) * stride];
-        const int diag = (blk - first) * VT;
-        const int cnt = min(VT, e0 - a0 - diag);
+        const int diag = (blk - first) * VO;
+        const int cnt = min(VO, e0 - a0 - diag);
         const int sa = split[blk];
         const int ea = (blk + 1 < next) ? split[blk + 1] : (b0 - a0);
-        merge_block<T, VT, STABLE>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag);
+        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag);
     }
     __syncthreads();
 }
 
 // Merges `nl` (a power of two <= 2*MAXP) lists held back to back in `src`
 // (list i = [off[i], off[i+1]), off[nl] = total) by log2(nl) rounds,
-// ping-ponging with `dst`. Returns the buffer holding the result. The lower
-// list wins ties in every round, so the result is ordered by (key, list).
+// ping-ponging with `dst` (both unpadded). Returns the buffer holding the
+// result. The lower list wins ties in every round, so the result is ordered by
+// (key, list).
 template <class T, int NT, int VT, int MAXP, bool STABLE>
 __device__ T* merge_lists(T* src, T* dst, const int* off, int nl, int* split) {
     for (int r = 0; (nl >> r) > 1; ++r) {
-        merge_round_lists<T, NT, VT, MAXP, STABLE>(src, dst, off, 1 << r, nl >> (r + 1), split);
+        merge_round_lists<T, NT, VT, MAXP, STABLE, LinIdx>(src, dst, off, 1 << r, nl >> (r + 1), split);
         T* t = src;
         src = dst;
         dst = t;

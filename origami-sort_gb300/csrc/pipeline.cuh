@@ -22,34 +22,36 @@ struct Config;
 // that a merge tile never straddles two run pairs.
 template <>
 struct Config<uint32_t> {
-    static constexpr int K1_NT = 256, K1_VT = 32;  // 8192-item tiles (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 16;    // 4096-item merge tiles
+    static constexpr int K1_NT = 512, K1_VTS = 16, K1_VTM = 32;  // 8192-item tiles (32 KiB)
+    static constexpr int M_NT = 256, M_VT = 16;                   // 4096-item merge tiles
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<uint64_t> {
-    static constexpr int K1_NT = 256, K1_VT = 16;  // 4096 items (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 8;    // 2048
+    static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;  // 4096 items (32 KiB)
+    static constexpr int M_NT = 256, M_VT = 8;                   // 2048
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<KV64> {
-    static constexpr int K1_NT = 256, K1_VT = 8;  // 2048 items (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 8;    // 2048
+    static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 7;  // 2048 items (32 KiB)
+    static constexpr int M_NT = 256, M_VT = 8;                  // 2048
     static constexpr bool STABLE = true;
 };
 
 template <class T>
+using K1Shape = BlockSortShape<T, Config<T>::K1_NT, Config<T>::K1_VTS, Config<T>::K1_VTM, Config<T>::STABLE>;
+template <class T>
 constexpr int k1_tile() {
-    return Config<T>::K1_NT * Config<T>::K1_VT;
+    return K1Shape<T>::TILE;
 }
 template <class T>
 constexpr int merge_tile() {
     return Config<T>::M_NT * Config<T>::M_VT;
 }
 template <class T>
-constexpr size_t k1_smem() {  // two padded tile buffers (merge rounds ping-pong)
-    return 2 * (size_t)padded_items<T>(k1_tile<T>() + Config<T>::K1_VT) * sizeof(T);
+constexpr size_t k1_smem() {
+    return K1Shape<T>::SMEM;
 }
 template <class T>
 constexpr size_t merge_smem() {
@@ -156,7 +158,7 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
 
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VT, C::STABLE>,
+        cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         cudaFuncSetAttribute(pair_merge_kernel<T, C::M_NT, C::M_VT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
@@ -172,7 +174,7 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
     launch(n_k1.c_str(), st, [&] {
-        block_sort_kernel<T, C::K1_NT, C::K1_VT, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
+        block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
             d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
     });
     if (stats) {

@@ -11,23 +11,32 @@
 namespace origami {
 
 // ---------------------------------------------------------------- K1 -----
-// Sorts tiles of NT*VT items. Restates the reference's phase 1 + phase 2
+// Sorts tiles of NT*VTS items. Restates the reference's phase 1 + phase 2
 // (sorter.h:3831-3849: in-register networks, then binary merges up to the
-// in-cache block size): each thread sorts VT items in registers, then
-// log2(NT) merge rounds in shared memory (merge_core.cuh) double the run length
-// until the tile (or the chunk) is sorted.
+// in-cache block size): each thread sorts VTS items in registers, then merge
+// rounds in shared memory (merge_core.cuh, VTM-register blocks) double the run
+// length until the tile (or the chunk) is sorted.
 // `chunk` (power of two) caps the sorted run length for chunked sorts.
 // xin/xout are the key masks applied on load / on store (sign flip for i64).
-template <class T, int NT, int VT, bool STABLE>
+template <class T, int NT, int VTS, int VTM, bool STABLE>
+struct BlockSortShape {
+    static constexpr int TILE = NT * VTS;
+    static constexpr int BUF = padded_items<T>(TILE + VTM + 1);  // items per buffer
+    static constexpr int VO = Block<T, VTM, STABLE>::VO;
+    static constexpr int SPLITS = TILE / VO + TILE / (2 * VTS) + 4;
+    static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
+};
+
+template <class T, int NT, int VTS, int VTM, bool STABLE>
 __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                         uint64_t n, int chunk, uint64_t xin,
                                                         uint64_t xout) {
-    constexpr int TILE = NT * VT;
-    constexpr int BUF = padded_items<T>(TILE + VT);
+    using Sh = BlockSortShape<T, NT, VTS, VTM, STABLE>;
+    constexpr int TILE = Sh::TILE;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sa = reinterpret_cast<T*>(smem_raw);
-    T* sb = sa + BUF;
-    __shared__ int split[TILE / VT + 1];
+    T* sb = reinterpret_cast<T*>(smem_raw + Sh::SMEM / 2);
+    __shared__ int split[Sh::SPLITS];
     const int tid = threadIdx.x;
     const uint64_t base = (uint64_t)blockIdx.x * TILE;
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
@@ -35,33 +44,44 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
     // coalesced striped load; the tail of a partial tile is filled with the
     // largest item, which sorts after every real item (stably for key-value)
 #pragma unroll
-    for (int k = 0; k < VT; ++k) {
+    for (int k = 0; k < VTS; ++k) {
         const int i = k * NT + tid;
         sa[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
     }
     __syncthreads();
     {
-        T v[VT];
+        T v[VTS];
 #pragma unroll
-        for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(tid * VT + k)];
-        thread_sort<T, VT, STABLE>(v, chunk);
+        for (int k = 0; k < VTS; ++k) v[k] = sa[pad<T>(tid * VTS + k)];
+        thread_sort<T, VTS, STABLE>(v, chunk);
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < VT; ++k) sa[pad<T>(tid * VT + k)] = v[k];
+        for (int k = 0; k < VTS; ++k) sa[pad<T>(tid * VTS + k)] = v[k];
     }
     __syncthreads();
     T* src = sa;
-    T* dst = sb;
-    for (int w = VT; w < TILE && w < chunk; w <<= 1) {
-        merge_round_uniform<T, NT, VT, STABLE>(src, dst, w, TILE, split);
-        T* t = src;
-        src = dst;
-        dst = t;
-    }
+    if (VTS < TILE && VTS < chunk) {
+        // first round reads the padded blocked layout, later rounds are unpadded
+        merge_round_uniform<T, NT, VTM, STABLE, PadIdx<T>>(sa, sb, VTS, TILE, split);
+        src = sb;
+        T* dst = sa;
+        for (int w = 2 * VTS; w < TILE && w < chunk; w <<= 1) {
+            merge_round_uniform<T, NT, VTM, STABLE, LinIdx>(src, dst, w, TILE, split);
+            T* t = src;
+            src = dst;
+            dst = t;
+        }
 #pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const int i = k * NT + tid;
-        if (i < valid) out[base + i] = Traits<T>::flip(src[pad<T>(i)], xout);
+        for (int k = 0; k < VTS; ++k) {
+            const int i = k * NT + tid;
+            if (i < valid) out[base + i] = Traits<T>::flip(src[i], xout);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VTS; ++k) {
+            const int i = k * NT + tid;
+            if (i < valid) out[base + i] = Traits<T>::flip(src[pad<T>(i)], xout);
+        }
     }
 }
 
