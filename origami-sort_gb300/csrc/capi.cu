@@ -174,7 +174,7 @@ int check_args(int kind, const void* d, const void* tmp, uint64_t n, uint64_t so
 // Merge fan-in for a min_k request: 2 keeps binary passes, 3..16 round up to
 // a power of two, larger values are capped at 16; 0 selects the default.
 int fan_of(unsigned min_k) {
-    if (min_k == 0) return 16;
+    if (min_k == 0) return 2;  // tuned default: binary passes are the fastest path today
     if (min_k <= 2) return 2;
     int f = 4;
     while ((unsigned)f < min_k && f < 16) f <<= 1;

@@ -176,25 +176,27 @@ template <>
 struct KwayCfg<uint32_t> {
     static constexpr int NT = 256, VT = 32, S = 32, TMAX = 8704;
     static constexpr int RANGE = 1 << 17;
+    static constexpr bool STABLE = false;
 };
 template <>
 struct KwayCfg<uint64_t> {
     static constexpr int NT = 256, VT = 16, S = 32, TMAX = 4096;
     static constexpr int RANGE = 1 << 16;
+    static constexpr bool STABLE = false;
 };
 template <>
 struct KwayCfg<KV64> {
     static constexpr int NT = 256, VT = 7, S = 16, TMAX = 1792;
     static constexpr int RANGE = 1 << 15;
+    static constexpr bool STABLE = true;
 };
 
 // Shared memory: three unpadded tile buffers (the tile being merged, the next
 // one arriving by cp.async, and a merge scratch), then the per-range tables.
 // While the range's samples are merged the three buffers serve as two halves
 // of the sample ping-pong.
-template <class T>
+template <class T, class C = KwayCfg<T>>
 struct KwayLayout {
-    using C = KwayCfg<T>;
     using K = typename Traits<T>::Key;
     using E = SampleE<K>;
     static constexpr int EVT = 7;  // sample merge: serial blocks of 7
@@ -207,7 +209,7 @@ struct KwayLayout {
     static constexpr size_t TAB_BYTES =
         (size_t)(MAXTILES + 1) * KWAY_MAX * 4 * 2 + (size_t)(MAXTILES + 1) * (KWAY_MAX + 1) * 4;
     static constexpr size_t SMEM = 3 * BUF_BYTES + TAB_BYTES + 64;
-    static constexpr int VO = Block<T, C::VT, Traits<T>::kStable>::VO;
+    static constexpr int VO = Block<T, C::VT, C::STABLE>::VO;
     static constexpr int MAXBLK_T = C::TMAX / VO + KWAY_MAX + 2;
     static constexpr int MAXBLK_S = (C::RANGE / C::S) / EVT + KWAY_MAX + 2;
     static constexpr int MAXBLK = MAXBLK_T > MAXBLK_S ? MAXBLK_T : MAXBLK_S;
@@ -221,12 +223,12 @@ struct NoProbe {
 };
 
 // One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
-template <class T, class Probe = NoProbe>
-__global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
+template <class T, class C = KwayCfg<T>, class Probe = NoProbe>
+__global__ void __launch_bounds__(C::NT) range_merge_kernel(
     const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int F, int rpg,
     const int64_t* __restrict__ bnd, uint64_t xout, Probe probe = Probe()) {
-    using C = KwayCfg<T>;
-    using Lay = KwayLayout<T>;
+    static_assert(C::STABLE || !Traits<T>::kStable, "key-value items need the stable merge");
+    using Lay = KwayLayout<T, C>;
     using K = typename Traits<T>::Key;
     using E = SampleE<K>;
     constexpr int NT = C::NT, VT = C::VT, S = C::S, M = Lay::M;
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(KwayCfg<T>::NT) range_merge_kernel(
         const int tot = to[KWAY_MAX];
         T* res = buf(cur);
         if (nl > 1)
-            res = merge_lists<T, NT, VT, KWAY_MAX / 2, Traits<T>::kStable>(buf(cur), buf(2), to, nl, mblk);
+            res = merge_lists<T, NT, C::VT, KWAY_MAX / 2, C::STABLE>(buf(cur), buf(2), to, nl, mblk);
         probe.mark(7);
         uint64_t ob = out_base;
         for (int q = 0; q < KWAY_MAX; ++q) ob += sp[t * KWAY_MAX + q];

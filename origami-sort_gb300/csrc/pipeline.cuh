@@ -22,40 +22,51 @@ struct Config;
 // that a merge tile never straddles two run pairs.
 template <>
 struct Config<uint32_t> {
-    static constexpr int K1_NT = 512, K1_VTS = 16, K1_VTM = 32;  // 8192-item tiles (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 16;                   // 4096-item merge tiles
+    // K1: warps sort 32*32 keys in registers, then shared-memory rounds to 8192
+    static constexpr bool WARP_K1 = true;
+    static constexpr int K1_NW = 8, K1_VT = 32;
+    static constexpr int K1_NT = 256, K1_VTS = 32, K1_VTM = 32;  // (block K1, unused)
+    static constexpr int P_NT = 288, P_VT = 32, P_TILE = 8192;    // binary pass tiles
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<uint64_t> {
-    static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;  // 4096 items (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 8;                   // 2048
+    static constexpr bool WARP_K1 = true;
+    static constexpr int K1_NW = 8, K1_VT = 16;
+    static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
+    static constexpr int P_NT = 288, P_VT = 16, P_TILE = 4096;
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<KV64> {
+    static constexpr bool WARP_K1 = false;  // key-value items need stable merges
+    static constexpr int K1_NW = 8, K1_VT = 8;
     static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 7;  // 2048 items (32 KiB)
-    static constexpr int M_NT = 256, M_VT = 8;                  // 2048
+    static constexpr int P_NT = 320, P_VT = 7, P_TILE = 2048;
     static constexpr bool STABLE = true;
 };
 
 template <class T>
 using K1Shape = BlockSortShape<T, Config<T>::K1_NT, Config<T>::K1_VTS, Config<T>::K1_VTM, Config<T>::STABLE>;
 template <class T>
+using K1WShape = WarpSortShape<T, Config<T>::K1_NW, Config<T>::K1_VT>;
+template <class T>
 constexpr int k1_tile() {
-    return K1Shape<T>::TILE;
+    return Config<T>::WARP_K1 ? K1WShape<T>::TILE : K1Shape<T>::TILE;
 }
 template <class T>
 constexpr int merge_tile() {
-    return Config<T>::M_NT * Config<T>::M_VT;
+    return Config<T>::P_TILE;
 }
 template <class T>
 constexpr size_t k1_smem() {
-    return K1Shape<T>::SMEM;
+    return Config<T>::WARP_K1 ? K1WShape<T>::SMEM : K1Shape<T>::SMEM;
 }
 template <class T>
+using PShape = PairShape<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::STABLE, Config<T>::P_TILE>;
+template <class T>
 constexpr size_t merge_smem() {
-    return (size_t)padded_items<T>(merge_tile<T>() + Config<T>::M_VT) * sizeof(T);
+    return PShape<T>::SMEM;
 }
 
 // Number of binary merge passes after K1 for runs to reach `limit` items.
@@ -158,9 +169,13 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
 
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
-        cudaFuncSetAttribute(pair_merge_kernel<T, C::M_NT, C::M_VT>,
+        if constexpr (C::WARP_K1)
+            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
+        else
+            cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
+        cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
         cudaFuncSetAttribute(range_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
@@ -174,8 +189,12 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
     launch(n_k1.c_str(), st, [&] {
-        block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
-            d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
+        if constexpr (C::WARP_K1)
+            warp_block_sort_kernel<T, C::K1_NW, C::K1_VT><<<(unsigned)tiles1, C::K1_NW * 32, k1_smem<T>(), st>>>(
+                d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
+        else
+            block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
+                d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
     });
     if (stats) {
         stats->kernels++;
@@ -193,7 +212,7 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
                 pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
             });
             launch(n_k3.c_str(), st, [&] {
-                pair_merge_kernel<T, C::M_NT, C::M_VT><<<(unsigned)tiles, C::M_NT, merge_smem<T>(), st>>>(
+                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE><<<(unsigned)tiles, C::P_NT, merge_smem<T>(), st>>>(
                     cur, nxt, n, run, splits, xo);
             });
             if (stats) stats->kernels += 2;

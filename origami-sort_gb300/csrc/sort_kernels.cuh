@@ -7,6 +7,7 @@
 #pragma once
 #include "common.cuh"
 #include "merge_core.cuh"
+#include "warp_sort.cuh"
 
 namespace origami {
 
@@ -85,6 +86,77 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
     }
 }
 
+// K1 for keys-only items: every warp sorts 32*VT keys entirely in registers
+// (lane network + shuffle merges, warp_sort.cuh), then merge rounds in shared
+// memory join the warps' runs into a tile of NW*32*VT keys.
+template <class T, int NW, int VT>
+struct WarpSortShape {
+    static constexpr int NT = NW * 32;
+    static constexpr int TILE = NT * VT;
+    static constexpr int WTILE = 32 * VT;
+    static constexpr int BUF = padded_items<T>(TILE + VT + 1);
+    static constexpr int VTM = VT;  // merge blocks of VT-1 outputs
+    static constexpr int SPLITS = TILE / (VTM - 1) + TILE / (2 * WTILE) + 4;
+    static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
+};
+
+template <class T, int NW, int VT>
+__global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __restrict__ in,
+                                                                 T* __restrict__ out, uint64_t n,
+                                                                 int chunk, uint64_t xin,
+                                                                 uint64_t xout) {
+    using Sh = WarpSortShape<T, NW, VT>;
+    constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sa = reinterpret_cast<T*>(smem_raw);
+    T* sb = reinterpret_cast<T*>(smem_raw + Sh::SMEM / 2);
+    __shared__ int split[Sh::SPLITS];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const uint64_t base = (uint64_t)blockIdx.x * TILE;
+    const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
+    const int w0 = warp * WT;
+
+    // coalesced load of the warp's slice, transposed to blocked order through
+    // the warp's part of shared memory (padded: conflict-free both ways)
+#pragma unroll
+    for (int k = 0; k < VT; ++k) {
+        const int i = w0 + k * 32 + lane;
+        sa[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
+    }
+    __syncwarp();
+    T v[VT];
+#pragma unroll
+    for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(w0 + lane * VT + k)];
+    warp_sort<T, VT>(v, chunk);
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+    __syncthreads();
+    if (WT < TILE && WT < chunk) {
+        merge_round_uniform<T, Sh::NT, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
+        T* src = sb;
+        T* dst = sa;
+        for (int w = 2 * WT; w < TILE && w < chunk; w <<= 1) {
+            merge_round_uniform<T, Sh::NT, VT, false, LinIdx>(src, dst, w, TILE, split);
+            T* t = src;
+            src = dst;
+            dst = t;
+        }
+#pragma unroll
+        for (int k = 0; k < VT; ++k) {
+            const int i = k * Sh::NT + tid;
+            if (i < valid) out[base + i] = Traits<T>::flip(src[i], xout);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VT; ++k) {
+            const int i = k * Sh::NT + tid;
+            if (i < valid) out[base + i] = Traits<T>::flip(sa[pad<T>(i)], xout);
+        }
+    }
+}
+
 // Geometry of one binary pass: runs of `run` items (the last one may be short)
 // are merged pairwise (2p, 2p+1) into runs of 2*run. Output tiles of `tile`
 // items never straddle a pair because 2*run is a multiple of tile.
@@ -118,17 +190,37 @@ __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uin
 
 // ---------------------------------------------------------------- K3 -----
 // Restates one level of the reference's binary merge (merger.h:4079-4218,
-// mergebl2_*) for one tile of output: the tile's slices of both runs are
-// staged in shared memory, every thread finds its diagonal by merge path and
-// merges VT items serially, and the tile is written back coalesced.
-template <class T, int NT, int VT>
+// mergebl2_*) for one tile of output: the tile's slices of both runs arrive
+// in shared memory by cp.async, one merge round (merge_core.cuh) merges them
+// and the tile is written back coalesced.
+template <class T, int NT, int VT, bool STABLE, int TILE>
+struct PairShape {
+    static constexpr int CAP = TILE + VT + 2;
+    static constexpr size_t BUF_BYTES = (((size_t)CAP * sizeof(T)) + 15) & ~(size_t)15;
+    static constexpr size_t SMEM = 2 * BUF_BYTES;
+    static constexpr int SPLITS = TILE / Block<T, VT, STABLE>::VO + 4;
+};
+
+template <class T>
+__device__ __forceinline__ void cp_async_one(T* smem, const T* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)));
+}
+
+template <class T, int NT, int VT, bool STABLE, int TILE>
 __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                         uint64_t n, uint64_t run,
                                                         const int64_t* __restrict__ splits,
                                                         uint64_t xout) {
-    constexpr int TILE = NT * VT;
+    using Sh = PairShape<T, NT, VT, STABLE, TILE>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s = reinterpret_cast<T*>(smem_raw);
+    T* s0 = reinterpret_cast<T*>(smem_raw);
+    T* s1 = reinterpret_cast<T*>(smem_raw + Sh::BUF_BYTES);
+    __shared__ int split[Sh::SPLITS];
+    __shared__ int off[3];
     const int tid = threadIdx.x;
     const uint64_t t = blockIdx.x;
     const uint64_t o = t * TILE;
@@ -146,23 +238,18 @@ __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ sr
     const T* A = src + g.pbase + a0;
     const T* B = src + g.pbase + g.la + b0;
 
-    for (int i = tid; i < total; i += NT) s[pad<T>(i)] = (i < na) ? A[i] : B[i - na];
-    __syncthreads();
-
-    T v[VT];
-    const int diag = tid * VT;
-    if (diag < total) {
-        const int a = smem_merge_path(s, 0, na, na, nb, diag);
-        smem_serial_merge<T, VT>(s, a, na, na + diag - a, total, v);
+    for (int i = tid; i < total; i += NT) cp_async_one(&s0[i], (i < na) ? A + i : B + (i - na));
+    asm volatile("cp.async.commit_group;\n" ::);
+    if (tid == 0) {
+        off[0] = 0;
+        off[1] = na;
+        off[2] = total;
     }
+    asm volatile("cp.async.wait_group 0;\n" ::);
     __syncthreads();
-    if (diag < total) {
-#pragma unroll
-        for (int k = 0; k < VT; ++k) s[pad<T>(diag + k)] = v[k];
-    }
-    __syncthreads();
+    merge_round_lists<T, NT, VT, 1, STABLE, LinIdx>(s0, s1, off, 1, 1, split);
     T* out = dst + o;
-    for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(s[pad<T>(i)], xout);
+    for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(s1[i], xout);
 }
 
 }  // namespace origami
