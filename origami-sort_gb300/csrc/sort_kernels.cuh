@@ -197,7 +197,7 @@ template <class T, int NT, int VT, bool STABLE, int TILE>
 struct PairShape {
     static constexpr int CAP = TILE + VT + 2;
     static constexpr size_t BUF_BYTES = (((size_t)CAP * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr size_t SMEM = 2 * BUF_BYTES;
+    static constexpr size_t SMEM = 3 * BUF_BYTES;
     static constexpr int SPLITS = TILE / Block<T, VT, STABLE>::VO + 4;
 };
 
@@ -210,46 +210,62 @@ __device__ __forceinline__ void cp_async_one(T* smem, const T* gmem) {
         asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)));
 }
 
+// Persistent form: CTA b handles tiles b, b + G, b + 2G, ... (G = grid size).
+// Three shared buffers: two inputs (the tile being merged and the next tile,
+// arriving by cp.async meanwhile) and the merge output.
 template <class T, int NT, int VT, bool STABLE, int TILE>
 __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                         uint64_t n, uint64_t run,
                                                         const int64_t* __restrict__ splits,
-                                                        uint64_t xout) {
+                                                        uint64_t ntiles, uint64_t xout) {
     using Sh = PairShape<T, NT, VT, STABLE, TILE>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s0 = reinterpret_cast<T*>(smem_raw);
-    T* s1 = reinterpret_cast<T*>(smem_raw + Sh::BUF_BYTES);
+    auto buf = [&](int i) { return reinterpret_cast<T*>(smem_raw + (size_t)i * Sh::BUF_BYTES); };
     __shared__ int split[Sh::SPLITS];
-    __shared__ int off[3];
+    __shared__ int off[2][3];
     const int tid = threadIdx.x;
-    const uint64_t t = blockIdx.x;
-    const uint64_t o = t * TILE;
-    const PairGeom g(o, n, run);
-    const uint64_t d0 = o - g.pbase;
-    const uint64_t pair_end = g.la + g.lb;
-    const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
-    const int64_t a0 = splits[t];
-    const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
-    const int64_t b0 = (int64_t)d0 - a0;
-    const int64_t b1 = (int64_t)d1 - a1;
-    const int na = (int)(a1 - a0);
-    const int nb = (int)(b1 - b0);
-    const int total = na + nb;
-    const T* A = src + g.pbase + a0;
-    const T* B = src + g.pbase + g.la + b0;
 
-    for (int i = tid; i < total; i += NT) cp_async_one(&s0[i], (i < na) ? A + i : B + (i - na));
+    // stage tile t into buffer slot `slot`: its A and B slices back to back
+    auto issue = [&](uint64_t t, int slot) {
+        const uint64_t o = t * TILE;
+        const PairGeom g(o, n, run);
+        const uint64_t d0 = o - g.pbase;
+        const uint64_t pair_end = g.la + g.lb;
+        const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
+        const int64_t a0 = splits[t];
+        const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
+        const int na = (int)(a1 - a0);
+        const int total = (int)(d1 - d0);
+        const T* A = src + g.pbase + a0;
+        const T* B = src + g.pbase + g.la + ((int64_t)d0 - a0);
+        T* s = buf(slot);
+        for (int i = tid; i < total; i += NT) cp_async_one(&s[i], (i < na) ? A + i : B + (i - na));
+        if (tid == 0) {
+            off[slot][0] = 0;
+            off[slot][1] = na;
+            off[slot][2] = total;
+        }
+    };
+
+    uint64_t t = blockIdx.x;
+    int slot = 0;
+    if (t < ntiles) issue(t, 0);
     asm volatile("cp.async.commit_group;\n" ::);
-    if (tid == 0) {
-        off[0] = 0;
-        off[1] = na;
-        off[2] = total;
+    for (; t < ntiles; t += gridDim.x) {
+        const uint64_t nx = t + gridDim.x;
+        if (nx < ntiles) issue(nx, slot ^ 1);
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group 1;\n" ::);
+        __syncthreads();
+        merge_round_lists<T, NT, VT, 1, STABLE, LinIdx>(buf(slot), buf(2), off[slot], 1, 1, split);
+        const int total = off[slot][2];
+        T* out = dst + t * TILE;
+        const T* r = buf(2);
+        for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(r[i], xout);
+        __syncthreads();
+        slot ^= 1;
     }
     asm volatile("cp.async.wait_group 0;\n" ::);
-    __syncthreads();
-    merge_round_lists<T, NT, VT, 1, STABLE, LinIdx>(s0, s1, off, 1, 1, split);
-    T* out = dst + o;
-    for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(s1[i], xout);
 }
 
 }  // namespace origami
