@@ -208,6 +208,31 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
         if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
         return ORIGAMI_OK;
     }
+    // the kernels move 16-byte vectors: caller buffers that are not 16-byte
+    // aligned are sorted in aligned arena copies
+    if ((((uintptr_t)d) | ((uintptr_t)tmp)) & 15) {
+        const uint64_t bytes = n * item_bytes(kind);
+        void* ad = nullptr;
+        void* at = nullptr;
+        CK(cudaMallocAsync(&ad, bytes, st), "aligned staging");
+        cudaError_t e0 = cudaMallocAsync(&at, bytes, st);
+        if (e0 != cudaSuccess) {
+            cudaFreeAsync(ad, st);
+            return cuda_fail(e0, "aligned staging");
+        }
+        void* r = nullptr;
+        int rc = ORIGAMI_OK;
+        e0 = cudaMemcpyAsync(ad, d, bytes, cudaMemcpyDeviceToDevice, st);
+        if (e0 == cudaSuccess) rc = sort_device_impl(kind, ad, at, n, sort_n, min_k, 0, &r, st);
+        if (e0 == cudaSuccess && rc == ORIGAMI_OK)
+            e0 = cudaMemcpyAsync(in_tmp ? tmp : d, r, bytes, cudaMemcpyDeviceToDevice, st);
+        cudaFreeAsync(ad, st);
+        cudaFreeAsync(at, st);
+        if (rc != ORIGAMI_OK) return rc;
+        if (e0 != cudaSuccess) return cuda_fail(e0, "aligned staging copy");
+        if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
+        return ORIGAMI_OK;
+    }
     void* scratch = nullptr;
     if (!tmp) CK(cudaMallocAsync(&scratch, n * item_bytes(kind), st), "scratch allocation");
     const int fan = fan_of(min_k);

@@ -195,4 +195,35 @@ __device__ __forceinline__ void smem_serial_merge(const T* s, int ia, int aEnd, 
     }
 }
 
+// 16-byte vector view of items (all buffers the kernels touch are 16-byte
+// aligned: the C ABI stages misaligned caller buffers through aligned scratch).
+template <class T>
+struct Vec {
+    static constexpr int N = 16 / (int)sizeof(T);  // items per vector
+};
+
+// Asynchronous 16-byte global -> shared copy (cp.async.cg); both addresses
+// 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit_all() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Stages items [p, p + cnt) of a 16-byte aligned global array `g` into shared
+// memory with 16-byte copies: the enclosing aligned vectors are copied to
+// `s` (16-byte aligned), and the first item lands at s[return value]. Reads at
+// most one partial vector past either end, never outside the enclosing
+// 16-byte chunks (so never across a page). All NT threads call it.
+template <class T, int NT>
+__device__ __forceinline__ int stage_vec(T* s, const T* g, uint64_t p, int cnt) {
+    constexpr int V = Vec<T>::N;
+    const int lead = (int)(p % V);
+    const uint64_t p0 = p - lead;
+    const int nv = (lead + cnt + V - 1) / V;
+    for (int i = threadIdx.x; i < nv; i += NT) cp_async16(s + (size_t)i * V, g + p0 + (uint64_t)i * V);
+    return lead;
+}
+
 }  // namespace origami

@@ -70,24 +70,6 @@ constexpr size_t merge_smem() {
 }
 
 // Number of binary merge passes after K1 for runs to reach `limit` items.
-// Persistent grid of the pair-merge kernel: as many CTAs as fit on the device.
-template <class T>
-int pair_grid() {
-    static int g = 0;
-    if (g == 0) {
-        using C = Config<T>;
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per, pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE>, C::P_NT, merge_smem<T>());
-        g = sms * (per > 0 ? per : 1);
-    }
-    return g;
-}
-
 inline int merge_passes(uint64_t limit, uint64_t tile) {
     int p = 0;
     for (uint64_t r = tile; r < limit; r <<= 1) ++p;
@@ -229,10 +211,9 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
             launch(n_k4.c_str(), st, [&] {
                 pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
             });
-            const unsigned grid = (unsigned)(tiles < (uint64_t)pair_grid<T>() ? tiles : (uint64_t)pair_grid<T>());
             launch(n_k3.c_str(), st, [&] {
-                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE><<<grid, C::P_NT, merge_smem<T>(), st>>>(
-                    cur, nxt, n, run, splits, tiles, xo);
+                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE><<<(unsigned)tiles, C::P_NT, merge_smem<T>(), st>>>(
+                    cur, nxt, n, run, splits, xo);
             });
             if (stats) stats->kernels += 2;
         } else {

@@ -114,26 +114,38 @@ __global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __res
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const uint64_t base = (uint64_t)blockIdx.x * TILE;
+    static_assert(VT % Vec<T>::N == 0, "lanes load whole vectors");
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const int w0 = warp * WT;
 
-    // coalesced load of the warp's slice, transposed to blocked order through
-    // the warp's part of shared memory (padded: conflict-free both ways)
-#pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const int i = w0 + k * 32 + lane;
-        sa[pad<T>(i)] = (i < valid) ? Traits<T>::flip(in[base + i], xin) : Traits<T>::max_item();
-    }
-    __syncwarp();
+    // each lane loads its VT consecutive keys with 16-byte vector loads
+    // (blocked order; a partial tail is filled with the largest key)
+    constexpr int V = Vec<T>::N;
     T v[VT];
+    {
+        const int i0 = w0 + lane * VT;
+        const T* src = in + base + i0;
 #pragma unroll
-    for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(w0 + lane * VT + k)];
+        for (int j = 0; j < VT / V; ++j) {
+            if (i0 + (j + 1) * V <= valid) {
+                const uint4 q = *reinterpret_cast<const uint4*>(src + j * V);
+                const T* e = reinterpret_cast<const T*>(&q);
+#pragma unroll
+                for (int k = 0; k < V; ++k) v[j * V + k] = Traits<T>::flip(e[k], xin);
+            } else {
+#pragma unroll
+                for (int k = 0; k < V; ++k) {
+                    const int i = i0 + j * V + k;
+                    v[j * V + k] = (i < valid) ? Traits<T>::flip(src[j * V + k], xin) : Traits<T>::max_item();
+                }
+            }
+        }
+    }
     warp_sort<T, VT>(v, chunk);
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
-    __syncthreads();
     if (WT < TILE && WT < chunk) {
+#pragma unroll
+        for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+        __syncthreads();
         merge_round_uniform<T, Sh::NT, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
         T* src = sb;
         T* dst = sa;
@@ -143,16 +155,33 @@ __global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __res
             src = dst;
             dst = t;
         }
+        // coalesced 16-byte stores of the sorted tile
+        const int nvec = valid / V;
+        for (int i = tid; i < nvec; i += Sh::NT) {
+            const uint4 q = *reinterpret_cast<const uint4*>(src + (size_t)i * V);
+            T e[V];
+            const T* qe = reinterpret_cast<const T*>(&q);
 #pragma unroll
-        for (int k = 0; k < VT; ++k) {
-            const int i = k * Sh::NT + tid;
-            if (i < valid) out[base + i] = Traits<T>::flip(src[i], xout);
+            for (int k = 0; k < V; ++k) e[k] = Traits<T>::flip(qe[k], xout);
+            *reinterpret_cast<uint4*>(out + base + (size_t)i * V) = *reinterpret_cast<const uint4*>(e);
         }
+        for (int i = nvec * V + tid; i < valid; i += Sh::NT) out[base + i] = Traits<T>::flip(src[i], xout);
     } else {
+        // runs end at the warp (or chunk) size: each lane stores its own keys
+        const int i0 = w0 + lane * VT;
+        T* dp = out + base + i0;
 #pragma unroll
-        for (int k = 0; k < VT; ++k) {
-            const int i = k * Sh::NT + tid;
-            if (i < valid) out[base + i] = Traits<T>::flip(sa[pad<T>(i)], xout);
+        for (int j = 0; j < VT / V; ++j) {
+            if (i0 + (j + 1) * V <= valid) {
+                T e[V];
+#pragma unroll
+                for (int k = 0; k < V; ++k) e[k] = Traits<T>::flip(v[j * V + k], xout);
+                *reinterpret_cast<uint4*>(dp + j * V) = *reinterpret_cast<const uint4*>(e);
+            } else {
+#pragma unroll
+                for (int k = 0; k < V; ++k)
+                    if (i0 + j * V + k < valid) dp[j * V + k] = Traits<T>::flip(v[j * V + k], xout);
+            }
         }
     }
 }
@@ -195,77 +224,59 @@ __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uin
 // and the tile is written back coalesced.
 template <class T, int NT, int VT, bool STABLE, int TILE>
 struct PairShape {
-    static constexpr int CAP = TILE + VT + 2;
-    static constexpr size_t BUF_BYTES = (((size_t)CAP * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr size_t SMEM = 3 * BUF_BYTES;
+    // input: A part and B part each padded to whole 16-byte vectors (+ read slack)
+    static constexpr int V = Vec<T>::N;
+    static constexpr int IN_CAP = TILE + 4 * V + VT + 4;
+    static constexpr int OUT_CAP = TILE + 4;
+    static constexpr size_t IN_BYTES = (((size_t)IN_CAP * sizeof(T)) + 15) & ~(size_t)15;
+    static constexpr size_t OUT_BYTES = (((size_t)OUT_CAP * sizeof(T)) + 15) & ~(size_t)15;
+    static constexpr size_t SMEM = IN_BYTES + OUT_BYTES;
     static constexpr int SPLITS = TILE / Block<T, VT, STABLE>::VO + 4;
 };
 
-template <class T>
-__device__ __forceinline__ void cp_async_one(T* smem, const T* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    if constexpr (sizeof(T) == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)));
-}
-
-// Persistent form: CTA b handles tiles b, b + G, b + 2G, ... (G = grid size).
-// Three shared buffers: two inputs (the tile being merged and the next tile,
-// arriving by cp.async meanwhile) and the merge output.
 template <class T, int NT, int VT, bool STABLE, int TILE>
 __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                         uint64_t n, uint64_t run,
                                                         const int64_t* __restrict__ splits,
-                                                        uint64_t ntiles, uint64_t xout) {
+                                                        uint64_t xout) {
     using Sh = PairShape<T, NT, VT, STABLE, TILE>;
+    constexpr int V = Sh::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto buf = [&](int i) { return reinterpret_cast<T*>(smem_raw + (size_t)i * Sh::BUF_BYTES); };
+    T* sin = reinterpret_cast<T*>(smem_raw);
+    T* sout = reinterpret_cast<T*>(smem_raw + Sh::IN_BYTES);
     __shared__ int split[Sh::SPLITS];
-    __shared__ int off[2][3];
     const int tid = threadIdx.x;
-
-    // stage tile t into buffer slot `slot`: its A and B slices back to back
-    auto issue = [&](uint64_t t, int slot) {
-        const uint64_t o = t * TILE;
-        const PairGeom g(o, n, run);
-        const uint64_t d0 = o - g.pbase;
-        const uint64_t pair_end = g.la + g.lb;
-        const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
-        const int64_t a0 = splits[t];
-        const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
-        const int na = (int)(a1 - a0);
-        const int total = (int)(d1 - d0);
-        const T* A = src + g.pbase + a0;
-        const T* B = src + g.pbase + g.la + ((int64_t)d0 - a0);
-        T* s = buf(slot);
-        for (int i = tid; i < total; i += NT) cp_async_one(&s[i], (i < na) ? A + i : B + (i - na));
-        if (tid == 0) {
-            off[slot][0] = 0;
-            off[slot][1] = na;
-            off[slot][2] = total;
-        }
-    };
-
-    uint64_t t = blockIdx.x;
-    int slot = 0;
-    if (t < ntiles) issue(t, 0);
-    asm volatile("cp.async.commit_group;\n" ::);
-    for (; t < ntiles; t += gridDim.x) {
-        const uint64_t nx = t + gridDim.x;
-        if (nx < ntiles) issue(nx, slot ^ 1);
-        asm volatile("cp.async.commit_group;\n" ::);
-        asm volatile("cp.async.wait_group 1;\n" ::);
-        __syncthreads();
-        merge_round_lists<T, NT, VT, 1, STABLE, LinIdx>(buf(slot), buf(2), off[slot], 1, 1, split);
-        const int total = off[slot][2];
-        T* out = dst + t * TILE;
-        const T* r = buf(2);
-        for (int i = tid; i < total; i += NT) out[i] = Traits<T>::flip(r[i], xout);
-        __syncthreads();
-        slot ^= 1;
+    const uint64_t t = blockIdx.x;
+    const uint64_t o = t * TILE;
+    const PairGeom g(o, n, run);
+    const uint64_t d0 = o - g.pbase;
+    const uint64_t pair_end = g.la + g.lb;
+    const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
+    const int64_t a0 = splits[t];
+    const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
+    const int na = (int)(a1 - a0);
+    const int total = (int)(d1 - d0);
+    const int nb = total - na;
+    const uint64_t pa = g.pbase + (uint64_t)a0;
+    const uint64_t pb = g.pbase + g.la + (d0 - (uint64_t)a0);
+    // A staged at sin[0..], B at the next vector boundary after A's vectors
+    const int a_lead = stage_vec<T, NT>(sin, src, pa, na);
+    const int b_base = ((a_lead + na + V - 1) / V) * V;
+    const int b_lead = stage_vec<T, NT>(sin + b_base, src, pb, nb);
+    cp_async_commit_all();
+    cp_async_wait_all();
+    __syncthreads();
+    merge_pair_round<T, NT, VT, STABLE>(sin, a_lead, na, b_base + b_lead, nb, sout, split);
+    // output tile starts 16-byte aligned (o is a multiple of TILE)
+    T* out = dst + o;
+    const int nvec = total / V;
+    for (int i = tid; i < nvec; i += NT) {
+        T tmp[V];
+#pragma unroll
+        for (int k = 0; k < V; ++k) tmp[k] = Traits<T>::flip(sout[i * V + k], xout);
+        *reinterpret_cast<uint4*>(out + (size_t)i * V) = *reinterpret_cast<const uint4*>(tmp);
     }
-    asm volatile("cp.async.wait_group 0;\n" ::);
+    for (int i = nvec * V + tid; i < total; i += NT) out[i] = Traits<T>::flip(sout[i], xout);
 }
 
 }  // namespace origami
