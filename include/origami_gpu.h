@@ -150,6 +150,30 @@ int origami_profile_enable(int on);
 int origami_profile_report(char* buf, uint64_t cap);
 uint64_t origami_launch_count(void);
 
+/*
+ * Allocation-free sort (no counterpart in the reference, which never needs
+ * device memory). For callers that cannot allocate device memory during the
+ * call: code running while another allocator holds the GPU's free memory, code
+ * in a latency-critical loop that must not let an allocation stall the
+ * device, runtimes that forbid the CUDA allocator. The regular entry points
+ * take splitter scratch from the library's arena; this one uses a fixed
+ * array of ORIGAMI_NOALLOC_SPLIT_SLOTS 8-byte slots (4 MiB) compiled into the
+ * library's device image, held on every GPU that loads the library until the
+ * process exits.
+ *   - d and tmp: device buffers of n items, both required, 16-byte aligned;
+ *     same result-buffer convention and flags as origami_sort_device.
+ *   - n must not exceed origami_noalloc_max_items(kind) (ORIGAMI_ERR_INVALID
+ *     otherwise); binary merge passes are used (min_k = 2).
+ *   - The first call on a device looks up the array's device address; make it
+ *     before capturing this call into a CUDA graph.
+ *   - All calls share the one array: calls whose work overlaps on the GPU race
+ *     and must be serialized by the caller.
+ */
+#define ORIGAMI_NOALLOC_SPLIT_SLOTS 524288
+uint64_t origami_noalloc_max_items(int kind);
+int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n,
+                                int flags, void** result, void* stream);
+
 /* Device arena used by the host-pointer calls and by the serving loop. */
 int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */
 int origami_arena_trim(void);               /* return cached memory to the driver */

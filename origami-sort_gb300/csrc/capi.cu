@@ -287,6 +287,14 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
 
 }  // namespace
 
+namespace origami {
+int noalloc_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+int noalloc_check(int kind, const void* d, const void* tmp, uint64_t n, uint64_t sort_n,
+                  void** result) {
+    return check_args(kind, d, tmp, n, sort_n, result);
+}
+}  // namespace origami
+
 extern "C" {
 
 int origami_version(void) { return ORIGAMI_GPU_VERSION; }

@@ -75,6 +75,10 @@ def lib():
         L.origami_profile_report.restype = i
         L.origami_profile_report.argtypes = [ctypes.c_char_p, u64]
         L.origami_launch_count.restype = u64
+        L.origami_noalloc_max_items.restype = u64
+        L.origami_noalloc_max_items.argtypes = [i]
+        L.origami_sort_noalloc_device.restype = i
+        L.origami_sort_noalloc_device.argtypes = [i, vp, vp, u64, u64, i, ctypes.POINTER(vp), vp]
         _lib = L
     return _lib
 
