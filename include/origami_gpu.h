@@ -119,6 +119,26 @@ int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint
                                 uint64_t sort_n, void** result, void* stream);
 
 /*
+ * Batched segmented sort (no single counterpart in the reference: it extends
+ * the chunked sort of bench_sort_phases.cpp:1307-1425 to arbitrary, uneven
+ * chunks). Segment s is items [offsets[s], offsets[s+1]) of d; every segment
+ * is sorted independently and in place (the result is in d; tmp is scratch of
+ * n items). One persistent launch with a device work queue does all segments:
+ * short ones wholly in registers or shared memory, long ones through tile
+ * sorts and merge levels. Key-value segments are sorted stably.
+ *   _device: d, tmp, offsets are device memory, d and tmp 16-byte aligned,
+ *            offsets[nseg] == n, asynchronous on `stream`
+ *            (ORIGAMI_FLAG_SYNC waits and reports device-side errors:
+ *            ORIGAMI_ERR_INVALID for decreasing offsets, ORIGAMI_ERR_TIMEOUT
+ *            if a bounded wait ran out).
+ *   host:    d and offsets are host memory (offsets[0] == 0, n = offsets[nseg]);
+ *            returns when d holds the result.
+ */
+int origami_sort_segmented_device(int kind, void* d, void* tmp, const uint64_t* offsets,
+                                  uint64_t nseg, uint64_t n, int flags, void* stream);
+int origami_sort_segmented(int kind, void* d, const uint64_t* offsets, uint64_t nseg, int flags);
+
+/*
  * MergeTree::merge(X, endX, C, n, ...) (reference merge_tree.h:2792, 3410):
  * way-way merge of the sorted device streams [X[i], endX[i]) into C. X and endX
  * are HOST arrays of `way` device pointers (way <= 16). Ties go to the lower

@@ -358,6 +358,100 @@ int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint
     return sort_device_impl(kind, src, dst, n, sort_n, 2, flags, result, (cudaStream_t)stream);
 }
 
+// ------------------------------------------------------------ segmented --
+int origami_sort_segmented_device(int kind, void* d, void* tmp, const uint64_t* offsets,
+                                  uint64_t nseg, uint64_t n, int flags, void* stream) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (nseg == 0 || n == 0) return ORIGAMI_OK;
+    if (!d || !tmp || !offsets) return fail(ORIGAMI_ERR_INVALID, "d, tmp and offsets are required");
+    if (nseg >= (1ull << 32) - 1) return fail(ORIGAMI_ERR_INVALID, "too many segments");
+    if (n > (1ull << 40)) return fail(ORIGAMI_ERR_INVALID, "n is too large");
+    if ((((uintptr_t)d) | ((uintptr_t)tmp)) & 15)
+        return fail(ORIGAMI_ERR_ALIGN, "segmented sort needs 16-byte aligned device buffers");
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint64_t m = key_mask(kind);
+    int maxl = 0;
+    uint64_t bytes = 0;
+    int erro = 0;
+    switch (kind) {
+        case ORIGAMI_U32:
+            maxl = seg_levels_u32(n);
+            bytes = seg_scratch_bytes_u32(n, nseg, maxl);
+            erro = seg_err_offset_u32(n, nseg, maxl);
+            break;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64:
+            maxl = seg_levels_u64(n);
+            bytes = seg_scratch_bytes_u64(n, nseg, maxl);
+            erro = seg_err_offset_u64(n, nseg, maxl);
+            break;
+        default:
+            maxl = seg_levels_kv(n);
+            bytes = seg_scratch_bytes_kv(n, nseg, maxl);
+            erro = seg_err_offset_kv(n, nseg, maxl);
+            break;
+    }
+    void* scratch = nullptr;
+    CK(cudaMallocAsync(&scratch, bytes, st), "segmented scratch");
+    cudaError_t e;
+    switch (kind) {
+        case ORIGAMI_U32: e = seg_sort_u32(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: e = seg_sort_u64(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
+        default: e = seg_sort_kv(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
+    }
+    int herr = 0;
+    if (e == cudaSuccess && (flags & ORIGAMI_FLAG_SYNC)) {
+        e = cudaMemcpyAsync(&herr, static_cast<char*>(scratch) + erro, sizeof(int),
+                            cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "segmented sort");
+    if (herr == 1) return fail(ORIGAMI_ERR_TIMEOUT, "a merge job waited past its budget");
+    if (herr == 2) return fail(ORIGAMI_ERR_INVALID, "segment offsets decrease");
+    return ORIGAMI_OK;
+}
+
+int origami_sort_segmented(int kind, void* d, const uint64_t* offsets, uint64_t nseg, int flags) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (nseg == 0) return ORIGAMI_OK;
+    if (!offsets) return fail(ORIGAMI_ERR_INVALID, "offsets is NULL");
+    const uint64_t n = offsets[nseg];
+    if (offsets[0] != 0) return fail(ORIGAMI_ERR_INVALID, "offsets[0] must be 0");
+    for (uint64_t s = 0; s < nseg; ++s)
+        if (offsets[s + 1] < offsets[s]) return fail(ORIGAMI_ERR_INVALID, "segment offsets decrease");
+    if (n == 0) return ORIGAMI_OK;
+    if (!d) return fail(ORIGAMI_ERR_INVALID, "d is NULL");
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    (void)flags;
+    const uint64_t bytes = n * item_bytes(kind);
+    cudaStream_t st = worker_stream();
+    void *dd = nullptr, *dt = nullptr, *doff = nullptr;
+    CK(cudaMallocAsync(&dd, bytes, st), "arena allocation");
+    cudaError_t e = cudaMallocAsync(&dt, bytes, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&doff, (nseg + 1) * sizeof(uint64_t), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dd, d, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(doff, offsets, (nseg + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        rc = origami_sort_segmented_device(kind, dd, dt, static_cast<const uint64_t*>(doff), nseg, n,
+                                           ORIGAMI_FLAG_SYNC, st);
+        if (rc == ORIGAMI_OK) e = cudaMemcpyAsync(d, dd, bytes, cudaMemcpyDeviceToHost, st);
+    }
+    if (dd) cudaFreeAsync(dd, st);
+    if (dt) cudaFreeAsync(dt, st);
+    if (doff) cudaFreeAsync(doff, st);
+    cudaError_t es = cudaStreamSynchronize(st);
+    if (rc != ORIGAMI_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "segmented sort staging");
+    if (es != cudaSuccess) return cuda_fail(es, "stream sync");
+    return ORIGAMI_OK;
+}
+
 int origami_arena_reserve(uint64_t bytes) {
     int rc = ensure_device();
     if (rc != ORIGAMI_OK) return rc;

@@ -20,4 +20,17 @@ ORIGAMI_DECLARE_SORT(u64)
 ORIGAMI_DECLARE_SORT(kv)
 #undef ORIGAMI_DECLARE_SORT
 
+// Batched segmented sort (segmented.cuh): levels to plan for, scratch bytes,
+// the launch sequence, and where the error word sits inside the scratch.
+#define ORIGAMI_DECLARE_SEG(name)                                                                 \
+    int seg_levels_##name(uint64_t n);                                                           \
+    uint64_t seg_scratch_bytes_##name(uint64_t n, uint64_t nseg, int maxl);                      \
+    cudaError_t seg_sort_##name(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n, \
+                                uint64_t key_mask, void* scratch, int maxl, cudaStream_t st);     \
+    int seg_err_offset_##name(uint64_t n, uint64_t nseg, int maxl);
+ORIGAMI_DECLARE_SEG(u32)
+ORIGAMI_DECLARE_SEG(u64)
+ORIGAMI_DECLARE_SEG(kv)
+#undef ORIGAMI_DECLARE_SEG
+
 }  // namespace origami

@@ -1,6 +1,7 @@
 // Instantiation of the plain-sort pipeline for KV64 items.
 #include "dispatch.h"
 #include "pipeline.cuh"
+#include "seg_host.cuh"
 
 namespace origami {
 
@@ -12,6 +13,23 @@ cudaError_t sort_kv(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
 
 uint64_t scratch_bytes_kv(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<KV64>(n, sort_n, fan);
+}
+
+int seg_levels_kv(uint64_t n) { return seg_levels_for<KV64>(n) + 1; }
+
+uint64_t seg_scratch_bytes_kv(uint64_t n, uint64_t nseg, int maxl) {
+    return seg_scratch_bytes<KV64>(n, nseg, maxl);
+}
+
+cudaError_t seg_sort_kv(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
+                          uint64_t key_mask, void* scratch, int maxl, cudaStream_t st) {
+    return seg_sort<KV64>(static_cast<KV64*>(d), static_cast<KV64*>(tmp), off, nseg, n, key_mask, scratch,
+                          maxl, st);
+}
+
+int seg_err_offset_kv(uint64_t n, uint64_t nseg, int maxl) {
+    SegState s = seg_state<KV64>(nullptr, nullptr, n, nseg, maxl);
+    return (int)(reinterpret_cast<char*>(s.err) - static_cast<char*>(nullptr));
 }
 
 }  // namespace origami

@@ -1,6 +1,7 @@
 // Instantiation of the plain-sort pipeline for uint32_t items.
 #include "dispatch.h"
 #include "pipeline.cuh"
+#include "seg_host.cuh"
 
 namespace origami {
 
@@ -12,6 +13,23 @@ cudaError_t sort_u32(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t k
 
 uint64_t scratch_bytes_u32(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint32_t>(n, sort_n, fan);
+}
+
+int seg_levels_u32(uint64_t n) { return seg_levels_for<uint32_t>(n) + 1; }
+
+uint64_t seg_scratch_bytes_u32(uint64_t n, uint64_t nseg, int maxl) {
+    return seg_scratch_bytes<uint32_t>(n, nseg, maxl);
+}
+
+cudaError_t seg_sort_u32(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
+                          uint64_t key_mask, void* scratch, int maxl, cudaStream_t st) {
+    return seg_sort<uint32_t>(static_cast<uint32_t*>(d), static_cast<uint32_t*>(tmp), off, nseg, n, key_mask, scratch,
+                          maxl, st);
+}
+
+int seg_err_offset_u32(uint64_t n, uint64_t nseg, int maxl) {
+    SegState s = seg_state<uint32_t>(nullptr, nullptr, n, nseg, maxl);
+    return (int)(reinterpret_cast<char*>(s.err) - static_cast<char*>(nullptr));
 }
 
 }  // namespace origami

@@ -51,6 +51,10 @@ __device__ __forceinline__ void lane_group_merge(T (&v)[VT], int g) {
     const int lane = threadIdx.x & 31;
     // flip stage: item k of lane l meets item VT-1-k of lane l ^ (g-1)
     const bool lower = (lane & (g >> 1)) == 0;
+    if constexpr (VT == 1) {
+        const T a = __shfl_xor_sync(0xFFFFFFFFu, v[0], g - 1);
+        v[0] = min_max_sel(v[0], a, lower);
+    }
 #pragma unroll
     for (int k = 0; k < VT / 2; ++k) {
         const T a = __shfl_xor_sync(0xFFFFFFFFu, v[VT - 1 - k], g - 1);

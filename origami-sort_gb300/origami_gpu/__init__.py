@@ -75,6 +75,10 @@ def lib():
         L.origami_profile_report.restype = i
         L.origami_profile_report.argtypes = [ctypes.c_char_p, u64]
         L.origami_launch_count.restype = u64
+        L.origami_sort_segmented_device.restype = i
+        L.origami_sort_segmented_device.argtypes = [i, vp, vp, vp, u64, u64, i, vp]
+        L.origami_sort_segmented.restype = i
+        L.origami_sort_segmented.argtypes = [i, vp, vp, u64, i]
         L.origami_noalloc_max_items.restype = u64
         L.origami_noalloc_max_items.argtypes = [i]
         L.origami_sort_noalloc_device.restype = i
@@ -171,6 +175,28 @@ def merge_series(src, dst, merge_start, sort_n, kind=None, stream=None):
     check(lib().origami_merge_series_device(k, sp, dp, n, merge_start, sort_n, ctypes.byref(res),
                                             ctypes.c_void_p(s)))
     return dst if res.value == dp else src
+
+
+def sort_segmented(d, offsets, tmp=None, kind=None, stream=None, sync=True):
+    """Sort every segment [offsets[s], offsets[s+1]) of d independently, in place.
+
+    numpy d/offsets: host call (returns when d is sorted). CUDA tensors: d, tmp
+    (same size as d, allocated if None) and offsets (uint64/int64 tensor) on the
+    device; runs on `stream` and waits unless sync=False."""
+    k = _kind(d, kind)
+    if _is_torch(d):
+        import torch
+        if tmp is None:
+            tmp = torch.empty_like(d)
+        dp, n = _ptr_len(d, k)
+        nseg = offsets.numel() - 1
+        s = stream if stream is not None else torch.cuda.current_stream(d.device).cuda_stream
+        check(lib().origami_sort_segmented_device(k, dp, tmp.data_ptr(), offsets.data_ptr(), nseg, n,
+                                                  FLAG_SYNC if sync else 0, ctypes.c_void_p(s)))
+        return d
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    check(lib().origami_sort_segmented(k, d.ctypes.data, off.ctypes.data, len(off) - 1, 0))
+    return d
 
 
 def profile_enable(on=True):
