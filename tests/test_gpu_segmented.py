@@ -46,7 +46,7 @@ def make_items(kind, n, seed, dist="uniform"):
 
 def expected(a, off):
     keys = orc.keys_of(a)
-    seg = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    seg = np.repeat(np.arange(len(off) - 1), np.diff(np.asarray(off, dtype=np.int64)))
     return a[np.lexsort((keys, seg))]  # stable within each segment
 
 
