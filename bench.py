@@ -180,6 +180,54 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def short_workloads(torch):
+    """Batched and serving measurements carried on the headline line (shorter
+    runs than `--workload batched|serving`). Failures are reported, not raised."""
+    from origami_gpu import workloads as wl
+    out = {}
+    try:
+        out["batched"] = wl.batched(torch, steps=3, warmup=3)
+    except Exception as e:  # reported in the line
+        out["batched"] = {"error": repr(e)}
+    try:
+        sv = wl.serving(torch, rates=(100, 200, 400), duration_s=2.0, pool_size=64)
+        out["serving"] = sv
+        ok = [r for r in sv["rates"] if r["failed"] == 0]
+        if ok:
+            top = ok[-1]
+            out["latency"] = {"p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+                              "offered_rate_per_s": top["offered_rate"],
+                              "keys_per_s": top["keys_per_s"], "source": "serving loop"}
+    except Exception as e:
+        out["serving"] = {"error": repr(e)}
+    return out
+
+
+def run_workload(args, torch, world, rank):
+    """`--workload batched|serving`: that workload alone, one JSON line."""
+    from origami_gpu import workloads as wl
+    if rank != 0:
+        return
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.workload == "batched":
+        r = wl.batched(torch, steps=args.steps, warmup=args.warmup, loop_steps=2)
+        line = {"metric": "Gkeys/s batched segmented sort (65,536 uint32 arrays, one graph replay)",
+                "value": r["segmented_gkeys_s"], "unit": "Gkeys/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["segmented_graph_ms"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": {"workload": r["workload"], "l2": r["l2"]}, "detail": r}
+    else:
+        r = wl.serving(torch, rates=(100, 200, 400, 800, 1600), duration_s=4.0, pool_size=128)
+        best = max(r["rates"], key=lambda x: x["keys_per_s"])
+        line = {"metric": "serving throughput (keys/s) with p50/p99 latency",
+                "value": best["keys_per_s"] / 1e9, "unit": "Gkeys/s", "n_gpus": 1,
+                "steps": len(r["rates"]), "warmup": 1, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "mixed u32/u64/kv", "data": "synthetic",
+                "config": {"workload": r["workload"]}, "detail": r}
+    line["clocks"] = clocks.stop()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,6 +237,10 @@ def main():
     ap.add_argument("--n", type=int, default=N_KEYS)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched and serving measurements added to the line")
+    ap.add_argument("--workload", default="sort", choices=["sort", "batched", "serving"],
+                    help="sort: the headline line; batched / serving: that workload alone, in full")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -208,6 +260,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     og.lib()
+    if args.workload != "sort":
+        run_workload(args, torch, world, rank)
+        return
     n = args.n
     kind = og.U32
     dev = torch.device("cuda", local)
@@ -298,6 +353,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n)
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        del d, tmp, out
+        torch.cuda.empty_cache()
+        extras = short_workloads(torch)
+
     line = {
         "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -317,6 +378,7 @@ def main():
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        **extras,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -139,6 +139,23 @@ int origami_sort_segmented_device(int kind, void* d, void* tmp, const uint64_t* 
 int origami_sort_segmented(int kind, void* d, const uint64_t* offsets, uint64_t nseg, int flags);
 
 /*
+ * Segmented-sort plan (no counterpart in the reference): the launch sequence
+ * of origami_sort_segmented_device over FIXED device buffers d, tmp, offsets,
+ * recorded once into a CUDA graph with its own scratch. Each launch replays it
+ * on `stream` (no allocation, one graph launch); refill d between launches.
+ * status() waits for the stream and reports the last replay's device-side
+ * errors like ORIGAMI_FLAG_SYNC does. Same argument rules as the _device call;
+ * n and nseg must be > 0. Create the plan outside any other stream capture.
+ */
+typedef struct origami_seg_plan origami_seg_plan;
+int origami_seg_plan_create(int kind, void* d, void* tmp, const uint64_t* offsets, uint64_t nseg,
+                            uint64_t n, origami_seg_plan** out);
+int origami_seg_plan_launch(origami_seg_plan* p, void* stream);
+int origami_seg_plan_status(origami_seg_plan* p, void* stream);
+uint64_t origami_seg_plan_kernels(const origami_seg_plan* p); /* kernels per replay */
+int origami_seg_plan_destroy(origami_seg_plan* p);
+
+/*
  * MergeTree::merge(X, endX, C, n, ...) (reference merge_tree.h:2792, 3410):
  * way-way merge of the sorted device streams [X[i], endX[i]) into C. X and endX
  * are HOST arrays of `way` device pointers (way <= 16). Ties go to the lower
@@ -193,6 +210,58 @@ uint64_t origami_launch_count(void);
 uint64_t origami_noalloc_max_items(int kind);
 int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n,
                                 int flags, void** result, void* stream);
+
+/*
+ * Serving loop (no counterpart in the reference, whose callers sort one array
+ * per call). A server owns one worker thread that runs continuous batching:
+ *   - submit() queues a request: sort the `n` items of `kind` at `in` into
+ *     `out` (out == in or NULL: in place; otherwise the two must not overlap).
+ *     Each may be host pageable, host pinned or device memory, with any
+ *     alignment; n = 0 completes at once. Both buffers must stay valid, and
+ *     `out` untouched, until wait() returns for the request.
+ *   - Requests are admitted in arrival order while the HBM budget allows (a
+ *     batch reserves twice its items, its offsets and the segmented sort's
+ *     scratch) and fewer than max_inflight batches are on the GPU. The oldest
+ *     request that does not fit waits for running batches to return memory.
+ *   - Admitted requests of one kind are coalesced into one batched segmented
+ *     sort (at most max_batch_items items unless one request is larger). Each
+ *     batch runs on its own stream, so new batches overlap running ones.
+ *   - Results are identical to sorting each request alone (key-value requests
+ *     stably).
+ * Errors: ORIGAMI_ERR_OOM at submit for a request that can never fit the
+ * budget; ORIGAMI_ERR_BUSY when max_queue requests are pending (or, from
+ * cancel, when the request was already admitted); ORIGAMI_ERR_TIMEOUT from
+ * wait() when timeout_ms (< 0: no limit) passes first; ORIGAMI_ERR_CANCELLED
+ * from wait() for a cancelled request; a failed batch's status (OOM when the
+ * device could not supply the budgeted memory) from wait() for each of its
+ * requests. wait() collects a finished request: its id is unknown afterwards.
+ * Zero arguments to create() select the defaults: 120 GiB budget, 4 batches in
+ * flight, 2^28 items per batch, 2^20 pending requests. destroy() cancels what
+ * is pending, waits for the batches in flight and frees the server; no other
+ * call on it may be in progress.
+ */
+typedef struct origami_server origami_server;
+
+typedef struct origami_server_stats {
+    uint64_t submitted, completed, failed, cancelled; /* requests since create/reset */
+    uint64_t keys;                                    /* items of completed requests */
+    uint64_t batches;                                 /* segmented launches */
+    uint64_t pending;                                 /* requests waiting now */
+    uint64_t bytes_reserved, peak_bytes_reserved;     /* against the HBM budget */
+    uint64_t max_concurrent_batches;                  /* most batches in flight at once */
+    double p50_ms, p99_ms, max_ms;                    /* latency, submission to completion */
+    double keys_per_s; /* keys / (last completion - first submission) */
+} origami_server_stats;
+
+int origami_server_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
+                          uint64_t max_batch_items, uint64_t max_queue);
+int origami_server_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
+                          uint64_t* id);
+int origami_server_wait(origami_server* s, uint64_t id, int64_t timeout_ms);
+int origami_server_cancel(origami_server* s, uint64_t id);
+int origami_server_get_stats(origami_server* s, origami_server_stats* out);
+int origami_server_reset_stats(origami_server* s);
+int origami_server_destroy(origami_server* s);
 
 /* Device arena used by the host-pointer calls and by the serving loop. */
 int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */

@@ -40,7 +40,15 @@ cudaEvent_t take_event() {
 }
 }  // namespace
 
-bool profiling_on() { return g_prof_on.load(std::memory_order_relaxed); }
+namespace {
+thread_local bool t_capturing = false;
+}
+// Launches recorded into a CUDA graph are not bracketed by events: the graph
+// replays as one unit and is timed as one.
+bool profiling_on() { return g_prof_on.load(std::memory_order_relaxed) && !t_capturing; }
+void set_capturing(bool on) { t_capturing = on; }
+uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+void count_launches(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int prof_begin(const char* name, cudaStream_t st) {
@@ -293,6 +301,51 @@ int noalloc_check(int kind, const void* d, const void* tmp, uint64_t n, uint64_t
                   void** result) {
     return check_args(kind, d, tmp, n, sort_n, result);
 }
+int api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+int arena_init() { return ensure_device(); }
+
+SegPlan seg_plan(int kind, uint64_t n, uint64_t nseg) {
+    SegPlan p{};
+    switch (kind) {
+        case ORIGAMI_U32:
+            p.maxl = seg_levels_u32(n);
+            p.scratch_bytes = seg_scratch_bytes_u32(n, nseg, p.maxl);
+            p.err_offset = seg_err_offset_u32(n, nseg, p.maxl);
+            break;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64:
+            p.maxl = seg_levels_u64(n);
+            p.scratch_bytes = seg_scratch_bytes_u64(n, nseg, p.maxl);
+            p.err_offset = seg_err_offset_u64(n, nseg, p.maxl);
+            break;
+        default:
+            p.maxl = seg_levels_kv(n);
+            p.scratch_bytes = seg_scratch_bytes_kv(n, nseg, p.maxl);
+            p.err_offset = seg_err_offset_kv(n, nseg, p.maxl);
+            break;
+    }
+    return p;
+}
+
+void seg_prepare(int kind) {
+    switch (kind) {
+        case ORIGAMI_U32: seg_prepare_u32(); break;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: seg_prepare_u64(); break;
+        default: seg_prepare_kv(); break;
+    }
+}
+
+cudaError_t seg_launch(int kind, void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
+                       void* scratch, const SegPlan& p, cudaStream_t st) {
+    const uint64_t m = key_mask(kind);
+    switch (kind) {
+        case ORIGAMI_U32: return seg_sort_u32(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return seg_sort_u64(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
+        default: return seg_sort_kv(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
+    }
+}
 }  // namespace origami
 
 extern "C" {
@@ -371,40 +424,13 @@ int origami_sort_segmented_device(int kind, void* d, void* tmp, const uint64_t* 
     int rc = ensure_device();
     if (rc != ORIGAMI_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    const uint64_t m = key_mask(kind);
-    int maxl = 0;
-    uint64_t bytes = 0;
-    int erro = 0;
-    switch (kind) {
-        case ORIGAMI_U32:
-            maxl = seg_levels_u32(n);
-            bytes = seg_scratch_bytes_u32(n, nseg, maxl);
-            erro = seg_err_offset_u32(n, nseg, maxl);
-            break;
-        case ORIGAMI_U64:
-        case ORIGAMI_I64:
-            maxl = seg_levels_u64(n);
-            bytes = seg_scratch_bytes_u64(n, nseg, maxl);
-            erro = seg_err_offset_u64(n, nseg, maxl);
-            break;
-        default:
-            maxl = seg_levels_kv(n);
-            bytes = seg_scratch_bytes_kv(n, nseg, maxl);
-            erro = seg_err_offset_kv(n, nseg, maxl);
-            break;
-    }
+    const SegPlan plan = seg_plan(kind, n, nseg);
     void* scratch = nullptr;
-    CK(cudaMallocAsync(&scratch, bytes, st), "segmented scratch");
-    cudaError_t e;
-    switch (kind) {
-        case ORIGAMI_U32: e = seg_sort_u32(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
-        case ORIGAMI_U64:
-        case ORIGAMI_I64: e = seg_sort_u64(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
-        default: e = seg_sort_kv(d, tmp, offsets, nseg, n, m, scratch, maxl, st); break;
-    }
+    CK(cudaMallocAsync(&scratch, plan.scratch_bytes, st), "segmented scratch");
+    cudaError_t e = seg_launch(kind, d, tmp, offsets, nseg, n, scratch, plan, st);
     int herr = 0;
     if (e == cudaSuccess && (flags & ORIGAMI_FLAG_SYNC)) {
-        e = cudaMemcpyAsync(&herr, static_cast<char*>(scratch) + erro, sizeof(int),
+        e = cudaMemcpyAsync(&herr, static_cast<char*>(scratch) + plan.err_offset, sizeof(int),
                             cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }

@@ -27,10 +27,31 @@ ORIGAMI_DECLARE_SORT(kv)
     uint64_t seg_scratch_bytes_##name(uint64_t n, uint64_t nseg, int maxl);                      \
     cudaError_t seg_sort_##name(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n, \
                                 uint64_t key_mask, void* scratch, int maxl, cudaStream_t st);     \
-    int seg_err_offset_##name(uint64_t n, uint64_t nseg, int maxl);
+    int seg_err_offset_##name(uint64_t n, uint64_t nseg, int maxl);                               \
+    int seg_prepare_##name(); /* one-time kernel attributes; call outside stream capture */
 ORIGAMI_DECLARE_SEG(u32)
 ORIGAMI_DECLARE_SEG(u64)
 ORIGAMI_DECLARE_SEG(kv)
 #undef ORIGAMI_DECLARE_SEG
+
+// Kind-generic form of the above (capi.cu), shared by the C ABI and the
+// serving loop: the plan for n items in nseg segments, then the launch
+// sequence on `st` with caller-provided scratch of plan.scratch_bytes. The
+// device error word (0 ok, 1 a bounded wait ran out, 2 bad offsets) is the int
+// at scratch + plan.err_offset once the stream has passed the launch.
+struct SegPlan {
+    int maxl;
+    uint64_t scratch_bytes;
+    int err_offset;
+};
+SegPlan seg_plan(int kind, uint64_t n, uint64_t nseg);
+void seg_prepare(int kind);
+cudaError_t seg_launch(int kind, void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
+                       void* scratch, const SegPlan& p, cudaStream_t st);
+
+// capi.cu: sets the thread's last-error message; makes the stream-ordered pool
+// the caching device arena (returns an ORIGAMI_* status).
+int api_fail(int code, const char* msg);
+int arena_init();
 
 }  // namespace origami

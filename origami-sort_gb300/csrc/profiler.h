@@ -12,6 +12,11 @@ namespace origami {
 
 bool profiling_on();
 void count_launch();
+// CUDA-graph support: launches made while the calling thread captures a graph
+// are counted but not timed; a replay adds the graph's kernel count.
+void set_capturing(bool on);
+uint64_t launches_so_far();
+void count_launches(uint64_t k);
 // Records the begin event; returns a slot id (or -1 when profiling is off).
 int prof_begin(const char* name, cudaStream_t st);
 void prof_end(int slot, cudaStream_t st);

@@ -1,0 +1,515 @@
+// Serving loop: continuous batching of sort requests onto the batched
+// segmented sort.
+//
+// Clients submit requests (an input and an output buffer, which may be the
+// same; host pageable, host pinned or device memory; any kind, any length) and
+// wait for the sorted output. One worker thread owns the device side:
+//  * admission: pending requests are taken in arrival order while the HBM
+//    budget allows (a batch reserves its items twice, its offsets and the
+//    segmented sort's scratch) and fewer than `max_inflight` batches are on the
+//    device. The oldest request that does not fit waits until running batches
+//    finish and return their memory; nothing overtakes it.
+//  * coalescing: admitted requests of one kind form a batch. Their items are
+//    copied back to back into one arena block and sorted by one segmented
+//    launch, each request a segment.
+//  * overlap: each in-flight batch has its own stream. The copies and sort of a
+//    new batch overlap the batches already running; the pool stays cached (the
+//    stream-ordered allocator's release threshold is raised), so after warm-up a
+//    batch's arena block is recycled memory.
+//  * completion: the batch's results are copied back into the requests' own
+//    buffers. A host function on the stream marks the batch finished and wakes
+//    the worker, which releases the memory and the waiting clients.
+// Latency is per request, from submission to the moment its batch finished.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/origami_gpu.h"
+#include "dispatch.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+using origami::SegPlan;
+
+enum ReqState { PENDING = 0, RUNNING = 1, DONE = 2, CANCELLED = 3, FAILED = 4 };
+enum MemKind { MEM_PAGEABLE = 0, MEM_PINNED = 1, MEM_DEVICE = 2 };
+
+struct Request {
+    uint64_t id = 0;
+    int kind = 0;
+    const void* in = nullptr;
+    void* out = nullptr;
+    uint64_t n = 0;
+    int mem_out = MEM_PAGEABLE;
+    int state = PENDING;
+    int status = ORIGAMI_OK;
+    Clock::time_point t_submit, t_done;
+};
+
+uint64_t item_bytes(int kind) { return kind == ORIGAMI_U32 ? 4u : (kind <= ORIGAMI_I64 ? 8u : 16u); }
+uint64_t r256(uint64_t b) { return (b + 255) & ~255ull; }
+
+// Arena block of one batch: d | tmp | offsets | scratch, each 256-byte aligned.
+struct Layout {
+    uint64_t tmp, off, scratch, total;
+    SegPlan plan;
+};
+Layout layout(int kind, uint64_t items, uint64_t nseg) {
+    Layout l;
+    l.plan = origami::seg_plan(kind, items, nseg);
+    const uint64_t data = r256(items * item_bytes(kind));
+    l.tmp = data;
+    l.off = 2 * data;
+    l.scratch = l.off + r256((nseg + 1) * 8);
+    l.total = l.scratch + r256(l.plan.scratch_bytes);
+    return l;
+}
+
+int mem_kind(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return MEM_PAGEABLE;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return MEM_DEVICE;
+    if (a.type == cudaMemoryTypeHost) return MEM_PINNED;
+    return MEM_PAGEABLE;
+}
+
+}  // namespace
+
+struct origami_server;
+
+namespace {
+struct Batch {
+    origami_server* srv = nullptr;
+    int kind = 0;
+    std::vector<std::shared_ptr<Request>> reqs;
+    std::vector<uint64_t> off;
+    Layout lay{};
+    cudaStream_t stream = nullptr;
+    char* block = nullptr;
+    int* herr = nullptr;  // pinned copy of the device error word
+    int status = ORIGAMI_OK;
+    std::atomic<bool> finished{false};
+    bool abandoned = false;  // its stream failed before the completion marker ran
+    Clock::time_point t_end;
+};
+}  // namespace
+
+struct origami_server {
+    uint64_t budget = 0;
+    int max_inflight = 0;
+    uint64_t max_batch_items = 0;
+    uint64_t max_queue = 0;
+    int device = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    uint64_t gen = 0;  // bumped by every submission and every finished batch
+    std::deque<std::shared_ptr<Request>> pending;
+    std::map<uint64_t, std::shared_ptr<Request>> reqs;  // until the client's wait() collects them
+    uint64_t in_use = 0, peak_in_use = 0;
+    bool stop = false;
+    uint64_t next_id = 0;
+
+    // statistics since creation or the last reset (under mu)
+    std::vector<double> lat_ms;
+    uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, keys = 0, batches = 0;
+    uint64_t max_concurrent = 0;
+    bool have_first = false;
+    Clock::time_point t_first, t_last;
+
+    // worker state; `inflight` changes only with mu held
+    std::vector<std::unique_ptr<Batch>> inflight;
+    std::vector<cudaStream_t> streams;
+    std::vector<int*> err_words;
+    std::vector<std::unique_ptr<Batch>> abandoned;  // kept: a late marker may still touch them
+    std::thread worker;
+
+    uint64_t need(int kind, uint64_t items, uint64_t nseg) const { return layout(kind, items, nseg).total; }
+
+    static void CUDART_CB on_done(void* p) {
+        auto* b = static_cast<Batch*>(p);
+        b->t_end = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(b->srv->mu);
+            b->finished.store(true);
+            ++b->srv->gen;
+        }
+        b->srv->cv_work.notify_one();
+    }
+
+    // Takes the next batch from the pending queue (mu held). Returns null when
+    // nothing can be admitted now.
+    std::unique_ptr<Batch> admit() {
+        while (!pending.empty() && pending.front()->state == CANCELLED) pending.pop_front();
+        if (pending.empty()) return nullptr;
+        auto b = std::make_unique<Batch>();
+        b->srv = this;
+        b->kind = -1;
+        uint64_t items = 0;
+        for (auto it = pending.begin(); it != pending.end();) {
+            auto r = *it;
+            if (r->state == CANCELLED) {
+                it = pending.erase(it);
+                continue;
+            }
+            if (b->kind >= 0 && r->kind != b->kind) {
+                ++it;
+                continue;
+            }
+            if (!b->reqs.empty() && items + r->n > max_batch_items) break;
+            // the oldest request waits for memory rather than being overtaken,
+            // so a large request is never starved by a stream of small ones
+            if (in_use + need(r->kind, items + r->n, b->reqs.size() + 1) > budget) break;
+            b->kind = r->kind;
+            items += r->n;
+            r->state = RUNNING;
+            b->reqs.push_back(r);
+            it = pending.erase(it);
+        }
+        if (b->reqs.empty()) return nullptr;
+        b->off.assign(b->reqs.size() + 1, 0);
+        for (size_t i = 0; i < b->reqs.size(); ++i) b->off[i + 1] = b->off[i] + b->reqs[i]->n;
+        b->lay = layout(b->kind, items, b->reqs.size());
+        in_use += b->lay.total;
+        peak_in_use = std::max(peak_in_use, in_use);
+        ++batches;
+        return b;
+    }
+
+    // Enqueues a batch's copies, sort and completion marker (mu not held).
+    void launch(Batch& b) {
+        if (streams.empty()) {
+            cudaStream_t s = nullptr;
+            cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+            streams.push_back(s);
+        }
+        b.stream = streams.back();
+        streams.pop_back();
+        if (err_words.empty()) {
+            int* w = nullptr;
+            if (cudaHostAlloc(&w, sizeof(int), cudaHostAllocDefault) != cudaSuccess) w = nullptr;
+            err_words.push_back(w);
+        }
+        b.herr = err_words.back();
+        err_words.pop_back();
+        if (b.herr) *b.herr = 0;
+
+        const uint64_t ib = item_bytes(b.kind);
+        const uint64_t items = b.off.back();
+        const uint64_t nseg = b.reqs.size();
+        cudaError_t e = b.herr ? cudaSuccess : cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&b.block), b.lay.total, b.stream);
+        if (e != cudaSuccess) b.block = nullptr;
+        char* d = b.block;
+        uint64_t* doff = d ? reinterpret_cast<uint64_t*>(d + b.lay.off) : nullptr;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(doff, b.off.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, b.stream);
+        for (uint64_t i = 0; e == cudaSuccess && i < nseg; ++i) {
+            const Request& r = *b.reqs[i];
+            e = cudaMemcpyAsync(d + b.off[i] * ib, r.in, r.n * ib, cudaMemcpyDefault, b.stream);
+        }
+        if (e == cudaSuccess)
+            e = origami::seg_launch(b.kind, d, d + b.lay.tmp, doff, nseg, items, d + b.lay.scratch, b.lay.plan,
+                                    b.stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b.herr, d + b.lay.scratch + b.lay.plan.err_offset, sizeof(int),
+                                cudaMemcpyDeviceToHost, b.stream);
+        // pinned and device destinations are written on the stream; pageable
+        // ones are copied when the batch is retired, so this thread never
+        // blocks on a running sort
+        for (uint64_t i = 0; e == cudaSuccess && i < nseg; ++i) {
+            const Request& r = *b.reqs[i];
+            if (r.mem_out != MEM_PAGEABLE)
+                e = cudaMemcpyAsync(r.out, d + b.off[i] * ib, r.n * ib, cudaMemcpyDefault, b.stream);
+        }
+        if (e != cudaSuccess) b.status = e == cudaErrorMemoryAllocation ? ORIGAMI_ERR_OOM : ORIGAMI_ERR_CUDA;
+        if (cudaLaunchHostFunc(b.stream, on_done, &b) != cudaSuccess) {
+            cudaStreamSynchronize(b.stream);
+            if (b.status == ORIGAMI_OK) b.status = ORIGAMI_ERR_CUDA;
+            b.t_end = Clock::now();
+            std::lock_guard<std::mutex> lk(mu);
+            b.finished.store(true);
+            ++gen;
+        }
+    }
+
+    // Copies pageable results out, reads the device error word and returns the
+    // batch's memory (mu not held).
+    void retire(Batch& b) {
+        const uint64_t ib = item_bytes(b.kind);
+        if (b.status == ORIGAMI_OK && b.herr && *b.herr != 0)
+            b.status = *b.herr == 1 ? ORIGAMI_ERR_TIMEOUT : ORIGAMI_ERR_INVALID;
+        if (b.status == ORIGAMI_OK) {
+            for (size_t i = 0; i < b.reqs.size(); ++i) {
+                const Request& r = *b.reqs[i];
+                if (r.mem_out != MEM_PAGEABLE) continue;
+                cudaError_t e = cudaMemcpyAsync(r.out, b.block + b.off[i] * ib, r.n * ib,
+                                                cudaMemcpyDeviceToHost, b.stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(b.stream);
+                if (e != cudaSuccess) {
+                    b.status = ORIGAMI_ERR_CUDA;
+                    break;
+                }
+            }
+        }
+        if (b.abandoned) return;  // the stream is broken: keep its memory and stream out of reuse
+        if (b.block) cudaFreeAsync(b.block, b.stream);
+        streams.push_back(b.stream);
+        if (b.herr) err_words.push_back(b.herr);
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        uint64_t seen = ~0ull;
+        while (true) {
+            // retire finished batches
+            std::vector<std::unique_ptr<Batch>> fin;
+            for (size_t i = 0; i < inflight.size();) {
+                if (inflight[i]->finished.load()) {
+                    fin.push_back(std::move(inflight[i]));
+                    inflight.erase(inflight.begin() + i);
+                } else {
+                    ++i;
+                }
+            }
+            if (!fin.empty()) {
+                lk.unlock();
+                for (auto& b : fin) retire(*b);
+                lk.lock();
+                for (auto& b : fin) {
+                    in_use -= b->lay.total;
+                    for (auto& r : b->reqs) {
+                        r->state = b->status == ORIGAMI_OK ? DONE : FAILED;
+                        r->status = b->status;
+                        r->t_done = b->t_end;
+                        lat_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+                        if (b->status == ORIGAMI_OK) {
+                            ++completed;
+                            keys += r->n;
+                        } else {
+                            ++failed;
+                        }
+                    }
+                    if (b->t_end > t_last) t_last = b->t_end;
+                    if (b->abandoned) abandoned.push_back(std::move(b));
+                }
+                cv_done.notify_all();
+            }
+            // admit and launch
+            std::vector<std::unique_ptr<Batch>> adm;
+            while ((int)(inflight.size() + adm.size()) < max_inflight) {
+                auto b = admit();
+                if (!b) break;
+                adm.push_back(std::move(b));
+            }
+            if (!adm.empty()) {
+                lk.unlock();
+                for (auto& b : adm) launch(*b);
+                lk.lock();
+                for (auto& b : adm) inflight.push_back(std::move(b));
+                max_concurrent = std::max<uint64_t>(max_concurrent, inflight.size());
+                continue;
+            }
+            if (!fin.empty()) continue;
+            if (stop && inflight.empty()) break;  // destroy() cancelled everything pending
+            // sleep until a submission or a finished batch; the timeout is a
+            // backstop that also notices streams that failed
+            if (gen == seen) {
+                cv_work.wait_for(lk, std::chrono::milliseconds(2), [&] { return gen != seen || stop; });
+                if (gen == seen && !inflight.empty()) {
+                    for (auto& b : inflight) {
+                        const cudaError_t q = cudaStreamQuery(b->stream);
+                        if (q != cudaSuccess && q != cudaErrorNotReady && !b->finished.load()) {
+                            b->abandoned = true;
+                            b->status = ORIGAMI_ERR_CUDA;
+                            b->t_end = Clock::now();
+                            b->finished.store(true);
+                            ++gen;
+                        }
+                    }
+                }
+            }
+            seen = gen;
+        }
+        lk.unlock();
+        for (cudaStream_t s : streams) cudaStreamDestroy(s);
+        for (int* w : err_words)
+            if (w) cudaFreeHost(w);
+        streams.clear();
+        err_words.clear();
+    }
+};
+
+extern "C" {
+
+int origami_server_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
+                          uint64_t max_batch_items, uint64_t max_queue) {
+    if (!out) return origami::api_fail(ORIGAMI_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    const int rc = origami::arena_init();
+    if (rc != ORIGAMI_OK) return rc;
+    auto* s = new origami_server();
+    s->budget = hbm_budget_bytes ? hbm_budget_bytes : (120ull << 30);
+    s->max_inflight = max_inflight > 0 ? max_inflight : 4;
+    s->max_batch_items = max_batch_items ? max_batch_items : (1ull << 28);
+    s->max_queue = max_queue ? max_queue : (1ull << 20);
+    cudaGetDevice(&s->device);
+    s->worker = std::thread([s] { s->run(); });
+    *out = s;
+    return ORIGAMI_OK;
+}
+
+int origami_server_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
+                          uint64_t* id) {
+    if (!s || !id) return origami::api_fail(ORIGAMI_ERR_INVALID, "server and id are required");
+    *id = 0;
+    if (kind < ORIGAMI_U32 || kind > ORIGAMI_KVU64) return origami::api_fail(ORIGAMI_ERR_DTYPE, "unknown item kind");
+    if (!out) out = const_cast<void*>(in);
+    if (n > 0 && !in) return origami::api_fail(ORIGAMI_ERR_INVALID, "input is NULL");
+    if (n > (1ull << 36)) return origami::api_fail(ORIGAMI_ERR_INVALID, "request is too large");
+    if (n > 0 && out != in) {
+        const char* a = static_cast<const char*>(in);
+        const char* c = static_cast<const char*>(out);
+        const uint64_t bytes = n * item_bytes(kind);
+        if (a < c + bytes && c < a + bytes)
+            return origami::api_fail(ORIGAMI_ERR_INVALID, "input and output overlap without being the same buffer");
+    }
+    auto r = std::make_shared<Request>();
+    r->kind = kind;
+    r->in = in;
+    r->out = out;
+    r->n = n;
+    r->mem_out = n ? mem_kind(out) : MEM_PAGEABLE;
+    r->t_submit = Clock::now();
+    const uint64_t alone = n ? s->need(kind, n, 1) : 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return origami::api_fail(ORIGAMI_ERR_CANCELLED, "server is shutting down");
+    if (alone > s->budget) return origami::api_fail(ORIGAMI_ERR_OOM, "request exceeds the HBM budget");
+    if (s->pending.size() >= s->max_queue) return origami::api_fail(ORIGAMI_ERR_BUSY, "request queue is full");
+    r->id = ++s->next_id;
+    ++s->submitted;
+    if (!s->have_first) {
+        s->have_first = true;
+        s->t_first = r->t_submit;
+    }
+    s->reqs[r->id] = r;
+    *id = r->id;
+    if (n == 0) {
+        r->state = DONE;
+        r->t_done = r->t_submit;
+        s->lat_ms.push_back(0.0);
+        ++s->completed;
+        s->cv_done.notify_all();
+        return ORIGAMI_OK;
+    }
+    s->pending.push_back(r);
+    ++s->gen;
+    s->cv_work.notify_one();
+    return ORIGAMI_OK;
+}
+
+int origami_server_wait(origami_server* s, uint64_t id, int64_t timeout_ms) {
+    if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return origami::api_fail(ORIGAMI_ERR_INVALID, "unknown request id");
+    auto r = it->second;
+    auto ready = [&] { return r->state >= DONE; };
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, ready);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+        return origami::api_fail(ORIGAMI_ERR_TIMEOUT, "request not finished yet");
+    }
+    s->reqs.erase(r->id);
+    if (r->state == CANCELLED) return origami::api_fail(ORIGAMI_ERR_CANCELLED, "request was cancelled");
+    if (r->status != ORIGAMI_OK) return origami::api_fail(r->status, "the request's batch failed");
+    return ORIGAMI_OK;
+}
+
+int origami_server_cancel(origami_server* s, uint64_t id) {
+    if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return origami::api_fail(ORIGAMI_ERR_INVALID, "unknown request id");
+    if (it->second->state != PENDING) return origami::api_fail(ORIGAMI_ERR_BUSY, "request already admitted");
+    it->second->state = CANCELLED;
+    ++s->cancelled;
+    s->cv_done.notify_all();
+    return ORIGAMI_OK;
+}
+
+int origami_server_get_stats(origami_server* s, origami_server_stats* out) {
+    if (!s || !out) return origami::api_fail(ORIGAMI_ERR_INVALID, "server and out are required");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::vector<double> l = s->lat_ms;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+        if (l.empty()) return 0.0;
+        const size_t i = (size_t)(q * (double)(l.size() - 1) + 0.5);
+        return l[std::min(i, l.size() - 1)];
+    };
+    std::memset(out, 0, sizeof *out);
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->cancelled = s->cancelled;
+    out->keys = s->keys;
+    out->batches = s->batches;
+    out->pending = s->pending.size();
+    out->bytes_reserved = s->in_use;
+    out->peak_bytes_reserved = s->peak_in_use;
+    out->max_concurrent_batches = s->max_concurrent;
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    out->max_ms = l.empty() ? 0.0 : l.back();
+    const double sec = s->have_first ? std::chrono::duration<double>(s->t_last - s->t_first).count() : 0.0;
+    out->keys_per_s = sec > 0 ? (double)s->keys / sec : 0.0;
+    return ORIGAMI_OK;
+}
+
+int origami_server_reset_stats(origami_server* s) {
+    if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->lat_ms.clear();
+    s->submitted = s->completed = s->failed = s->cancelled = s->keys = s->batches = 0;
+    s->max_concurrent = s->inflight.size();
+    s->peak_in_use = s->in_use;
+    s->have_first = false;
+    s->t_last = Clock::time_point();
+    return ORIGAMI_OK;
+}
+
+int origami_server_destroy(origami_server* s) {
+    if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto& r : s->pending)
+            if (r->state == PENDING) {
+                r->state = CANCELLED;
+                ++s->cancelled;
+            }
+        s->pending.clear();
+        s->stop = true;
+        ++s->gen;
+    }
+    s->cv_work.notify_all();
+    s->cv_done.notify_all();
+    s->worker.join();
+    delete s;
+    return ORIGAMI_OK;
+}
+
+}  // extern "C"

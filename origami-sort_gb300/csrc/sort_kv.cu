@@ -27,6 +27,8 @@ cudaError_t seg_sort_kv(void* d, void* tmp, const uint64_t* off, uint64_t nseg, 
                           maxl, st);
 }
 
+int seg_prepare_kv() { return seg_grid<KV64>(); }
+
 int seg_err_offset_kv(uint64_t n, uint64_t nseg, int maxl) {
     SegState s = seg_state<KV64>(nullptr, nullptr, n, nseg, maxl);
     return (int)(reinterpret_cast<char*>(s.err) - static_cast<char*>(nullptr));

@@ -27,6 +27,8 @@ cudaError_t seg_sort_u32(void* d, void* tmp, const uint64_t* off, uint64_t nseg,
                           maxl, st);
 }
 
+int seg_prepare_u32() { return seg_grid<uint32_t>(); }
+
 int seg_err_offset_u32(uint64_t n, uint64_t nseg, int maxl) {
     SegState s = seg_state<uint32_t>(nullptr, nullptr, n, nseg, maxl);
     return (int)(reinterpret_cast<char*>(s.err) - static_cast<char*>(nullptr));

@@ -27,6 +27,8 @@ cudaError_t seg_sort_u64(void* d, void* tmp, const uint64_t* off, uint64_t nseg,
                           maxl, st);
 }
 
+int seg_prepare_u64() { return seg_grid<uint64_t>(); }
+
 int seg_err_offset_u64(uint64_t n, uint64_t nseg, int maxl) {
     SegState s = seg_state<uint64_t>(nullptr, nullptr, n, nseg, maxl);
     return (int)(reinterpret_cast<char*>(s.err) - static_cast<char*>(nullptr));

@@ -40,6 +40,17 @@ class OrigamiError(RuntimeError):
         self.code = code
 
 
+class ServerStats(ctypes.Structure):
+    """origami_server_stats (include/origami_gpu.h)."""
+    _fields_ = [(f, ctypes.c_uint64) for f in (
+        "submitted", "completed", "failed", "cancelled", "keys", "batches", "pending",
+        "bytes_reserved", "peak_bytes_reserved", "max_concurrent_batches")] + \
+        [(f, ctypes.c_double) for f in ("p50_ms", "p99_ms", "max_ms", "keys_per_s")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -83,6 +94,30 @@ def lib():
         L.origami_noalloc_max_items.argtypes = [i]
         L.origami_sort_noalloc_device.restype = i
         L.origami_sort_noalloc_device.argtypes = [i, vp, vp, u64, u64, i, ctypes.POINTER(vp), vp]
+        L.origami_server_create.restype = i
+        L.origami_server_create.argtypes = [ctypes.POINTER(vp), u64, i, u64, u64]
+        L.origami_server_submit.restype = i
+        L.origami_server_submit.argtypes = [vp, i, vp, vp, u64, ctypes.POINTER(u64)]
+        L.origami_server_wait.restype = i
+        L.origami_server_wait.argtypes = [vp, u64, ctypes.c_int64]
+        L.origami_server_cancel.restype = i
+        L.origami_server_cancel.argtypes = [vp, u64]
+        L.origami_server_get_stats.restype = i
+        L.origami_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+        L.origami_server_reset_stats.restype = i
+        L.origami_server_reset_stats.argtypes = [vp]
+        L.origami_server_destroy.restype = i
+        L.origami_server_destroy.argtypes = [vp]
+        L.origami_seg_plan_create.restype = i
+        L.origami_seg_plan_create.argtypes = [i, vp, vp, vp, u64, u64, ctypes.POINTER(vp)]
+        L.origami_seg_plan_launch.restype = i
+        L.origami_seg_plan_launch.argtypes = [vp, vp]
+        L.origami_seg_plan_status.restype = i
+        L.origami_seg_plan_status.argtypes = [vp, vp]
+        L.origami_seg_plan_kernels.restype = u64
+        L.origami_seg_plan_kernels.argtypes = [vp]
+        L.origami_seg_plan_destroy.restype = i
+        L.origami_seg_plan_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -197,6 +232,96 @@ def sort_segmented(d, offsets, tmp=None, kind=None, stream=None, sync=True):
     off = np.ascontiguousarray(offsets, dtype=np.uint64)
     check(lib().origami_sort_segmented(k, d.ctypes.data, off.ctypes.data, len(off) - 1, 0))
     return d
+
+
+class SegmentedPlan:
+    """CUDA-graph plan of a segmented sort over fixed device tensors
+    (origami_seg_plan_*): launch() replays it on a stream."""
+
+    def __init__(self, d, offsets, tmp, kind):
+        self.kind = _kind(d, kind)
+        dp, n = _ptr_len(d, self.kind)
+        h = ctypes.c_void_p()
+        check(lib().origami_seg_plan_create(self.kind, dp, tmp.data_ptr(), offsets.data_ptr(),
+                                            offsets.numel() - 1, n, ctypes.byref(h)))
+        self._h = h
+        self._keep = (d, offsets, tmp)
+
+    @property
+    def kernels(self):
+        return int(lib().origami_seg_plan_kernels(self._h))
+
+    def launch(self, stream):
+        check(lib().origami_seg_plan_launch(self._h, ctypes.c_void_p(stream)))
+
+    def status(self, stream):
+        check(lib().origami_seg_plan_status(self._h, ctypes.c_void_p(stream)))
+
+    def close(self):
+        if self._h is not None:
+            check(lib().origami_seg_plan_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (origami_server_* in include/origami_gpu.h).
+
+    submit(x, out=None) queues a sort of x (numpy array, possibly pinned, or a
+    CUDA tensor with kind=) into out (default: in place) and returns a request
+    id; wait(id) blocks until it is sorted. The caller keeps both buffers alive,
+    and out untouched, until wait() returns."""
+
+    def __init__(self, hbm_budget_bytes=0, max_inflight=0, max_batch_items=0, max_queue=0):
+        h = ctypes.c_void_p()
+        check(lib().origami_server_create(ctypes.byref(h), hbm_budget_bytes, max_inflight,
+                                          max_batch_items, max_queue))
+        self._h = h
+
+    def submit(self, x, out=None, kind=None):
+        """Queue a sort of x into `out` (None: in place); returns the request id."""
+        k = _kind(x, kind)
+        p, n = _ptr_len(x, k)
+        q = p if out is None else _ptr_len(out, k)[0]
+        rid = ctypes.c_uint64()
+        check(lib().origami_server_submit(self._h, k, p, q, n, ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1):
+        check(lib().origami_server_wait(self._h, rid, timeout_ms))
+
+    def cancel(self, rid):
+        check(lib().origami_server_cancel(self._h, rid))
+
+    def stats(self):
+        st = ServerStats()
+        check(lib().origami_server_get_stats(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def reset_stats(self):
+        check(lib().origami_server_reset_stats(self._h))
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            check(lib().origami_server_destroy(self._h))
+        self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def profile_enable(on=True):

@@ -80,3 +80,16 @@ def test_python_surface_raises_without_fallback(lib):
     with pytest.raises(og.OrigamiError) as e:
         og.sort_single_thread(np.arange(10, dtype=np.uint32), np.zeros(10, np.uint32))
     assert e.value.code == og.ERR_NO_DEVICE
+
+
+def test_server_without_device(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert lib.origami_server_create(ctypes.byref(h), 0, 0, 0, 0) == og.ERR_NO_DEVICE
+    assert not h.value
+    assert lib.origami_server_create(None, 0, 0, 0, 0) == og.ERR_INVALID
+    st = og.ServerStats()
+    assert lib.origami_server_get_stats(None, ctypes.byref(st)) == og.ERR_INVALID
+    assert lib.origami_server_destroy(None) == og.ERR_INVALID

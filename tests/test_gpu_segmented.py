@@ -121,3 +121,25 @@ def test_segmented_rejects_decreasing_offsets():
     with pytest.raises(og.OrigamiError) as e:
         og.sort_segmented(d, o, kind=og.U32)
     assert e.value.code == og.ERR_INVALID
+
+
+@pytest.mark.parametrize("kind", [og.U32, og.I64, og.KV64])
+def test_segmented_graph_plan(kind):
+    rng = np.random.default_rng(40 + kind)
+    lens = lengths(kind, rng, 200)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    a = make_items(kind, int(off[-1]), seed=kind + 50)
+    d = torch.from_numpy(a.view(np.uint8).copy()).cuda()
+    tmp = torch.empty_like(d)
+    o = torch.from_numpy(off.astype(np.int64)).cuda()
+    src = d.clone()
+    plan = og.SegmentedPlan(d, o, tmp, kind=kind)
+    assert plan.kernels == 4
+    s = torch.cuda.current_stream().cuda_stream
+    want = expected(a, off)
+    for _ in range(3):  # replays over refilled input
+        d.copy_(src)
+        plan.launch(s)
+        plan.status(s)
+        assert np.array_equal(d.cpu().numpy().view(a.dtype), want)
+    plan.close()
