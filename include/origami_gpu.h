@@ -157,9 +157,13 @@ int origami_seg_plan_destroy(origami_seg_plan* p);
 
 /*
  * MergeTree::merge(X, endX, C, n, ...) (reference merge_tree.h:2792, 3410):
- * way-way merge of the sorted device streams [X[i], endX[i]) into C. X and endX
- * are HOST arrays of `way` device pointers (way <= 16). Ties go to the lower
- * stream, so the merge is stable across streams.
+ * way-way merge of the sorted device streams [X[i], endX[i]) into C (any way;
+ * up to 16 streams take one HBM pass, more take one pass per factor of 16).
+ * X and endX are HOST arrays of `way` device pointers; C receives all items
+ * (the reference aligns C down to its register block first; here C is used
+ * as given). Streams must be aligned to the item size (16 bytes for key-value
+ * items) and must not overlap C. Ties go to the lower stream, so the merge is
+ * stable across streams. Asynchronous on `stream`.
  */
 int origami_merge_tree_device(int kind, void* const* X, void* const* endX, void* C, unsigned way,
                               void* stream);
@@ -170,7 +174,10 @@ int origami_merge_tree_device(int kind, void* const* X, void* const* endX, void*
  * [L[i], R[i]) and each requested output rank ranks[j] (host array, count
  * n_ranks), writes split offsets splits[j*K + i] (host array) such that taking
  * the first splits[j*K+i] items of every stream gives exactly the ranks[j]
- * smallest items, ties ordered by stream. K <= 16.
+ * smallest items, ties ordered by stream. K <= 1024. Waits for `stream`.
+ * Partition_Ptrs(L, R, S, K) is this call with one rank: the sum of the
+ * caller's initial S[k] - L[k]; the reference then moves S to the same split
+ * whenever the keys at the boundary are distinct.
  */
 int origami_partition_device(int kind, void* const* L, void* const* R, unsigned K,
                              const uint64_t* ranks, uint64_t n_ranks, uint64_t* splits,
@@ -262,6 +269,19 @@ int origami_server_cancel(origami_server* s, uint64_t id);
 int origami_server_get_stats(origami_server* s, origami_server_stats* out);
 int origami_server_reset_stats(origami_server* s);
 int origami_server_destroy(origami_server* s);
+
+/*
+ * Device-side input generator for the reference's Writer distributions
+ * (writer.h:27-35; no device counterpart there): fills the device buffer d
+ * with n items of `kind`, dist 1..9 = uniform, all same, sorted, reverse
+ * sorted, almost sorted (every 7th item at the maximum), Pareto keys, Pareto
+ * back to back, Pareto shuffled, Fibonacci. Distributions 2, 6, 7 and 9 are
+ * the reference's exact sequences; 1, 3, 4, 5 draw from a counter-based
+ * generator seeded by `seed` (the reference's std::mt19937 stream is
+ * sequential) with the reference's value ranges; 8 shuffles 7 with `seed`.
+ * Key-value items get value = key + 1. Asynchronous on `stream`.
+ */
+int origami_generate_device(int kind, void* d, uint64_t n, int dist, uint64_t seed, void* stream);
 
 /* Device arena used by the host-pointer calls and by the serving loop. */
 int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */

@@ -85,11 +85,18 @@ def build(verbose=False, force=False, ptxas_info=False):
     tmp_so = SO + ".tmp"
     _run([nv, *ARCH, "-shared", "-o", tmp_so, *objs], verbose)
     os.replace(tmp_so, SO)
-    # C++ drivers linked against the library
+    # C++ drivers linked against the library and the CUDA runtime
+    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
+    cuda_lib = next((p for p in (os.path.join(cuda_home, "lib64"), os.path.join(cuda_home, "lib"))
+                     if os.path.isdir(p)), os.path.join(cuda_home, "lib64"))
+    djobs = []
     for drv in sorted(glob.glob(os.path.join(DRIVERS, "*.cpp"))):
         exe = os.path.join(BIN, os.path.basename(drv)[:-4])
-        _run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"), drv, "-o", exe,
-              "-L" + LIB, "-lorigami_gpu", "-Wl,-rpath," + LIB, "-pthread"], verbose)
+        djobs.append(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"),
+                      "-I" + os.path.join(cuda_home, "include"), drv, "-o", exe, "-L" + LIB, "-lorigami_gpu",
+                      "-L" + cuda_lib, "-lcudart", "-Wl,-rpath," + LIB, "-Wl,-rpath," + cuda_lib, "-pthread"])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(djobs))) as ex:
+        list(ex.map(lambda c: _run(c, verbose), djobs))
     return SO
 
 

@@ -80,9 +80,56 @@ struct SplitGeom {
     }
 };
 
+// Where the sorted lists of merge group g live. Sort passes merge groups of F
+// consecutive runs of one array (RunLists); the merge-tree entry point merges
+// up to KWAY_MAX independent streams as one group (StreamLists). A group gives
+// list(i) / len(i) for its lists (len 0 past the last) and out_base(), the
+// group's first output position.
 template <class T>
-__global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ src, uint64_t n,
-                                                         uint64_t run, int F, int rpg,
+struct RunGroup {
+    const T* src;
+    uint64_t base, G, run;
+    int nr;
+    __device__ __forceinline__ const T* list(int i) const { return src + base + (uint64_t)i * run; }
+    __device__ __forceinline__ uint64_t len(int i) const {
+        const uint64_t s = (uint64_t)i * run;
+        return (i < nr) ? ((G - s) < run ? (G - s) : run) : 0;
+    }
+    __device__ __forceinline__ uint64_t out_base() const { return base; }
+};
+
+template <class T>
+struct RunLists {
+    const T* src;
+    uint64_t n, run;
+    int F;
+    __device__ __forceinline__ RunGroup<T> group(uint64_t g) const {
+        const SplitGeom geo(g, n, run, F);
+        return RunGroup<T>{src, geo.base, geo.G, run, geo.nr};
+    }
+};
+
+template <class T>
+struct StreamLists {
+    const T* ptr[KWAY_MAX];
+    uint64_t cnt[KWAY_MAX];
+    uint64_t G;  // sum of cnt
+    int nr;      // streams in use
+    __device__ __forceinline__ const StreamLists& group(uint64_t) const { return *this; }
+    __device__ __forceinline__ const T* list(int i) const { return ptr[i]; }
+    __device__ __forceinline__ uint64_t len(int i) const { return i < nr ? cnt[i] : 0; }
+    __device__ __forceinline__ uint64_t out_base() const { return 0; }
+};
+
+// Keys as compared: xin flips the sign bit of signed keys read straight from a
+// caller's buffer (0 for data the pipeline has already flipped).
+template <class T>
+__device__ __forceinline__ typename Traits<T>::Key ckey(const T& v, uint64_t xin) {
+    return Traits<T>::key(v) ^ (typename Traits<T>::Key)xin;
+}
+
+template <class T, class Lists>
+__global__ void __launch_bounds__(256) kway_split_kernel(const Lists lists, int rpg, uint64_t xin,
                                                          int64_t* __restrict__ bnd,
                                                          int* __restrict__ err) {
     using K = typename Traits<T>::Key;
@@ -92,19 +139,19 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ s
     const int tid = threadIdx.x;
     const uint64_t g = blockIdx.x / (uint64_t)(rpg + 1);
     const int b = (int)(blockIdx.x % (uint64_t)(rpg + 1));
-    const SplitGeom geo(g, n, run, F);
+    const auto& geo = lists.group(g);
     const uint64_t r = (uint64_t)(((unsigned __int128)b * geo.G) / (uint64_t)rpg);
     int64_t* out = bnd + (uint64_t)blockIdx.x * KWAY_MAX;
     if (tid < KWAY_MAX) {
-        const int64_t L = (int64_t)geo.len(tid, run);
+        const int64_t L = (int64_t)geo.len(tid);
         const int64_t others = (int64_t)geo.G - L;
         lo[tid] = (int64_t)r - others > 0 ? (int64_t)r - others : 0;
         hi[tid] = (int64_t)r < L ? (int64_t)r : L;
     }
     __syncthreads();
     const int j = tid >> 4, i = tid & 15;
-    const T* runj = src + geo.base + (uint64_t)j * run;
-    const T* runi = src + geo.base + (uint64_t)i * run;
+    const T* runj = geo.list(j);
+    const T* runi = geo.list(i);
     for (int round = 0; round < 80; ++round) {
         if (tid == 0) {
             int o = 0;
@@ -121,7 +168,7 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ s
         const bool probe = (j < geo.nr) && (loj < hij);
         const int64_t pj = loj + (hij - loj) / 2;
         K xk = 0;
-        if (probe && i == j) xk = Traits<T>::key(runj[pj]);
+        if (probe && i == j) xk = ckey(runj[pj], xin);
         xk = __shfl_sync(0xFFFFFFFFu, xk, (tid & 16) | j);
         int64_t c = 0;
         if (probe && i < geo.nr) {
@@ -132,7 +179,7 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const T* __restrict__ s
                 const bool le = i < j;  // earlier runs precede on equal keys
                 while (a < e) {
                     const int64_t mid = (a + e) >> 1;
-                    const K v = Traits<T>::key(runi[mid]);
+                    const K v = ckey(runi[mid], xin);
                     if (le ? (v <= xk) : (v < xk))
                         a = mid + 1;
                     else
@@ -223,10 +270,12 @@ struct NoProbe {
 };
 
 // One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
-template <class T, class C = KwayCfg<T>, class Probe = NoProbe>
+// xin: sign flip applied to items as they are read (signed keys straight from a
+// caller's buffer); xout: flip applied as they are written.
+template <class T, class Lists, class C = KwayCfg<T>, class Probe = NoProbe>
 __global__ void __launch_bounds__(C::NT) range_merge_kernel(
-    const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int F, int rpg,
-    const int64_t* __restrict__ bnd, uint64_t xout, Probe probe = Probe()) {
+    const Lists lists, T* __restrict__ dst, int rpg, const int64_t* __restrict__ bnd, uint64_t xin,
+    uint64_t xout, Probe probe = Probe()) {
     static_assert(C::STABLE || !Traits<T>::kStable, "key-value items need the stable merge");
     using Lay = KwayLayout<T, C>;
     using K = typename Traits<T>::Key;
@@ -240,7 +289,8 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     int* toff = reinterpret_cast<int*>(hist + (Lay::MAXTILES + 1) * KWAY_MAX);  // [MAXTILES+1][17]
     __shared__ int off[KWAY_MAX + 1];
     __shared__ int mblk[Lay::MAXBLK];  // merge-round block splits
-    __shared__ int64_t lo[KWAY_MAX];
+    __shared__ const T* lo[KWAY_MAX];  // first item of each list's slice of this range
+    __shared__ int64_t skip[KWAY_MAX];  // items of each list before the range
     __shared__ uint32_t len[KWAY_MAX];
     __shared__ uint64_t out_base;
     const int tid = threadIdx.x;
@@ -248,22 +298,23 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     // --- range geometry
     const uint64_t g = bnd ? blockIdx.x / (uint64_t)rpg : blockIdx.x;
     const int rb = bnd ? (int)(blockIdx.x % (uint64_t)rpg) : 0;
-    const SplitGeom geo(g, n, run, F);
+    const auto& geo = lists.group(g);
     if (tid < KWAY_MAX) {
-        const uint64_t L = geo.len(tid, run);
+        const uint64_t L = geo.len(tid);
         int64_t a = 0, e = (int64_t)L;
         if (bnd) {
             const int64_t* bb = bnd + ((uint64_t)g * (rpg + 1) + rb) * KWAY_MAX;
             a = bb[tid];
             e = bb[KWAY_MAX + tid];
         }
-        lo[tid] = (int64_t)(geo.base + (uint64_t)tid * run) + a;
+        lo[tid] = geo.list(tid) + a;
+        skip[tid] = a;
         len[tid] = (uint32_t)(e - a);
     }
     __syncthreads();
     if (tid == 0) {
-        uint64_t ob = geo.base;
-        for (int q = 0; q < KWAY_MAX; ++q) ob += (uint64_t)(lo[q] - (int64_t)(geo.base + (uint64_t)q * run));
+        uint64_t ob = geo.out_base();
+        for (int q = 0; q < KWAY_MAX; ++q) ob += (uint64_t)skip[q];
         out_base = ob;
         int o = 0;
         for (int q = 0; q < KWAY_MAX; ++q) {
@@ -282,11 +333,11 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     E* sB = reinterpret_cast<E*>(smem_raw + Lay::SBUF_BYTES);
     for (int q = 0; q < geo.nr; ++q) {
         const int c = off[q + 1] - off[q];
-        const T* rp = src + lo[q];
+        const T* rp = lo[q];
         const int o0 = off[q];
         for (int k = tid; k < c; k += NT) {
             E e;
-            e.key = Traits<T>::key(rp[(uint64_t)(k + 1) * S - 1]);
+            e.key = ckey(rp[(uint64_t)(k + 1) * S - 1], xin);
             e.tag = ((uint32_t)k << 4) | (uint32_t)q;
             sA[o0 + k] = e;
         }
@@ -332,11 +383,11 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
             } else {
                 uint32_t a = pj * S;
                 uint32_t e = min(a + (uint32_t)(S - 1), len[j]);
-                const T* rp = src + lo[j];
+                const T* rp = lo[j];
                 const bool le = j < gi;  // earlier runs precede on equal keys
                 while (a < e) {
                     const uint32_t mid = (a + e) >> 1;
-                    const K kv = Traits<T>::key(rp[mid]);
+                    const K kv = ckey(rp[mid], xin);
                     if (le ? (kv <= gs.key) : (kv < gs.key))
                         a = mid + 1;
                     else
@@ -366,7 +417,7 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
         for (int q = 0; q < geo.nr; ++q) {
             const int o0 = to[q];
             const int l = to[q + 1] - o0;
-            const T* rp = src + lo[q] + sp[t * KWAY_MAX + q];
+            const T* rp = lo[q] + sp[t * KWAY_MAX + q];
             for (int k = tid; k < l; k += NT) cp_async_item(&b[o0 + k], rp + k);
         }
         cp_async_commit();
@@ -385,6 +436,11 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
         probe.mark(6);
         const int* to = toff + t * (KWAY_MAX + 1);
         const int tot = to[KWAY_MAX];
+        if (xin) {  // flip signed keys of the arrived tile in place
+            T* tb = buf(cur);
+            for (int k = tid; k < tot; k += NT) tb[k] = Traits<T>::flip(tb[k], xin);
+            __syncthreads();
+        }
         T* res = buf(cur);
         if (nl > 1)
             res = merge_lists<T, NT, C::VT, KWAY_MAX / 2, C::STABLE>(buf(cur), buf(2), to, nl, mblk);

@@ -108,6 +108,8 @@ def lib():
         L.origami_server_reset_stats.argtypes = [vp]
         L.origami_server_destroy.restype = i
         L.origami_server_destroy.argtypes = [vp]
+        L.origami_generate_device.restype = i
+        L.origami_generate_device.argtypes = [i, vp, u64, i, u64, vp]
         L.origami_seg_plan_create.restype = i
         L.origami_seg_plan_create.argtypes = [i, vp, vp, vp, u64, u64, ctypes.POINTER(vp)]
         L.origami_seg_plan_launch.restype = i
@@ -322,6 +324,61 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+WRITER_DISTS = {"uniform": 1, "same": 2, "sorted": 3, "reverse": 4, "almost_sorted": 5,
+                "pareto": 6, "pareto_b2b": 7, "pareto_shuffled": 8, "fibonacci": 9}
+
+
+def generate(d, dist, kind, seed=0, stream=None):
+    """Fill the CUDA tensor d with a Writer distribution (writer.h:27-35) on the
+    device: dist is 1..9 or a name from WRITER_DISTS."""
+    import torch
+    k = _kind(d, kind)
+    p, n = _ptr_len(d, k)
+    dv = WRITER_DISTS[dist] if isinstance(dist, str) else int(dist)
+    s = stream if stream is not None else torch.cuda.current_stream(d.device).cuda_stream
+    check(lib().origami_generate_device(k, p, n, dv, seed, ctypes.c_void_p(s)))
+    return d
+
+
+def _stream_bounds(streams, k):
+    lo = [_ptr_len(t, k)[0] or 0 for t in streams]
+    hi = [p + _ptr_len(t, k)[1] * ITEM_BYTES[k] for p, t in zip(lo, streams)]
+    arr = ctypes.c_void_p * len(streams)
+    return arr(*lo), arr(*hi)
+
+
+def merge_tree(streams, out, kind, stream=None):
+    """MergeTree::merge(X, endX, C, n, ...) (merge_tree.h:2792): merge the sorted
+    CUDA tensors `streams` into `out` (ties: lower stream first)."""
+    import torch
+    k = _kind(out, kind)
+    X, E = _stream_bounds(streams, k)
+    s = stream if stream is not None else torch.cuda.current_stream(out.device).cuda_stream
+    check(lib().origami_merge_tree_device(k, X, E, out.data_ptr(), len(streams), ctypes.c_void_p(s)))
+    return out
+
+
+def partition(streams, ranks, kind, stream=None):
+    """Splits of the sorted CUDA tensors `streams` at each output rank:
+    an (n_ranks, K) array; ties are ordered by stream (Partition.h:118-166)."""
+    import torch
+    k = _kind(streams[0], kind)
+    L, R = _stream_bounds(streams, k)
+    rk = np.ascontiguousarray(ranks, dtype=np.uint64)
+    out = np.zeros((len(rk), len(streams)), np.uint64)
+    s = stream if stream is not None else torch.cuda.current_stream(streams[0].device).cuda_stream
+    check(lib().origami_partition_device(k, L, R, len(streams), rk.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                         len(rk), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                         ctypes.c_void_p(s)))
+    return out
+
+
+def partition_ptrs(streams, guesses, kind):
+    """partition_templated::Partition_Ptrs(L, R, S, K) (Partition.h:118): moves
+    the per-stream offsets `guesses` to the split of the same total rank."""
+    return [int(x) for x in partition(streams, [int(sum(guesses))], kind)[0]]
 
 
 def profile_enable(on=True):
