@@ -3,6 +3,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -258,6 +259,67 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
     return ORIGAMI_OK;
 }
 
+// Device view of a host buffer the GPU can address: the mapped pointer of
+// pinned memory, or the pointer itself for pageable memory when the device
+// reads it through the host's page tables (address translation services on
+// Grace). nullptr when neither applies or ORIGAMI_HOST_DIRECT=0.
+void* device_view(void* p) {
+    static const bool enabled = [] {
+        const char* e = std::getenv("ORIGAMI_HOST_DIRECT");
+        return !(e && e[0] == '0');
+    }();
+    if (!enabled) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered) {
+        int dev = 0, pageable = 0, host_tables = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+        if (pageable && host_tables) return p;
+    }
+    return nullptr;
+}
+
+int typed_io(int kind, const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n, int fan,
+             void* scratch, cudaStream_t st) {
+    const uint64_t m = key_mask(kind);
+    cudaError_t e;
+    switch (kind) {
+        case ORIGAMI_U32: e = sort_io_u32(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: e = sort_io_u64(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
+        default: e = sort_io_kv(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
+    }
+    return e == cudaSuccess ? ORIGAMI_OK : cuda_fail(e, "sort launch");
+}
+
+// Host buffers the device can address: the first kernel reads them over the
+// host link and the last pass writes the result straight back, so no copy
+// pass is made; the merge passes in between use two arena buffers.
+int sort_host_direct(int kind, const void* vin, void* vout, uint64_t n, uint64_t sort_n, unsigned min_k,
+                     cudaStream_t st) {
+    const uint64_t bytes = n * item_bytes(kind);
+    const int fan = fan_of(min_k);
+    void *wa = nullptr, *wb = nullptr, *work = nullptr;
+    CK(cudaMallocAsync(&wa, bytes, st), "arena allocation");
+    cudaError_t e = cudaMallocAsync(&wb, bytes, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&work, scratch_bytes(kind, n, sort_n, fan), st);
+    int rc = e == cudaSuccess ? typed_io(kind, vin, vout, wa, wb, n, sort_n, fan, work, st)
+                              : cuda_fail(e, "arena allocation");
+    if (work) cudaFreeAsync(work, st);
+    if (wb) cudaFreeAsync(wb, st);
+    cudaFreeAsync(wa, st);
+    const cudaError_t es = cudaStreamSynchronize(st);
+    if (rc != ORIGAMI_OK) return rc;
+    if (es != cudaSuccess) return cuda_fail(es, "stream sync");
+    return ORIGAMI_OK;
+}
+
 // Host buffers: stage through the arena, sort on the device, copy the result
 // back into d (or tmp) and return when it is there.
 int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
@@ -269,6 +331,12 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
     if (n == 0) return ORIGAMI_OK;
     const uint64_t bytes = n * item_bytes(kind);
     cudaStream_t st = worker_stream();
+    if (n > 1) {
+        void* vin = device_view(d);
+        void* vout = vin ? device_view(out) : nullptr;
+        if (vin && vout && !((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
+            return sort_host_direct(kind, vin, vout, n, sort_n, min_k, st);
+    }
     void* dd = nullptr;
     void* dt = nullptr;
     CK(cudaMallocAsync(&dd, bytes, st), "arena allocation");
@@ -548,18 +616,5 @@ int origami_profile_report(char* buf, uint64_t cap) {
 }
 
 uint64_t origami_launch_count(void) { return g_launches.load(); }
-
-int origami_merge_tree_device(int kind, void* const* X, void* const* endX, void* C, unsigned way,
-                              void* stream) {
-    (void)kind; (void)X; (void)endX; (void)C; (void)way; (void)stream;
-    return fail(ORIGAMI_ERR_INVALID, "merge tree entry point not built yet");
-}
-
-int origami_partition_device(int kind, void* const* L, void* const* R, unsigned K,
-                             const uint64_t* ranks, uint64_t n_ranks, uint64_t* splits,
-                             void* stream) {
-    (void)kind; (void)L; (void)R; (void)K; (void)ranks; (void)n_ranks; (void)splits; (void)stream;
-    return fail(ORIGAMI_ERR_INVALID, "partition entry point not built yet");
-}
 
 }  // extern "C"

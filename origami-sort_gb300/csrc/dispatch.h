@@ -14,7 +14,9 @@ struct LaunchStats;
     cudaError_t sort_##name(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, \
                             void* want, int fan, void* scratch, cudaStream_t st,                \
                             LaunchStats* stats);                                                \
-    uint64_t scratch_bytes_##name(uint64_t n, uint64_t sort_n, int fan);
+    uint64_t scratch_bytes_##name(uint64_t n, uint64_t sort_n, int fan);                          \
+    cudaError_t sort_io_##name(const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n, \
+                               uint64_t key_mask, int fan, void* scratch, cudaStream_t st);
 ORIGAMI_DECLARE_SORT(u32)
 ORIGAMI_DECLARE_SORT(u64)
 ORIGAMI_DECLARE_SORT(kv)

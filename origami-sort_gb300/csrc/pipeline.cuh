@@ -143,12 +143,19 @@ uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan) {
     return bytes + 256;
 }
 
-// Sorts d[0..n) in chunks of sort_n (0 = one full sort) into `want` (d or
-// tmp). `key_mask` is XORed into every key on the way in and on the way out.
+// Sorts in[0..n) in chunks of sort_n (0 = one full sort) into out[0..n).
+// The first kernel reads `in` once and the last pass writes `out` once; the
+// passes in between ping-pong between the work buffers wa and wb (the pass
+// before the last writes wa, the one before that wb, ...). `in` may be one of
+// the work buffers (the first kernel sorts tiles in place) and out may be wb;
+// in and out may also be host memory the device can address (pinned or, with
+// address translation services, pageable), which streams the data over the
+// host link inside the first and last kernels instead of separate copies.
+// `key_mask` is XORed into every key on the way in and on the way out.
 // `scratch` holds pipeline_scratch_bytes<T>(n, sort_n, fan) bytes of device memory.
 template <class T>
-cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, T* want,
-                          int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
+cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint64_t sort_n, uint64_t key_mask,
+                             int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
     using C = Config<T>;
     using KC = KwayCfg<T>;
     constexpr int T1 = k1_tile<T>();
@@ -159,10 +166,10 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
     const std::vector<PassPlan> plan = plan_passes<T>(n, limit, fan);
     const int passes = (int)plan.size();
     const int k1_chunk = (int)(limit < (uint64_t)T1 ? (full ? T1 : limit) : T1);
-    // the last writer must target `want`: with an even number of merge passes
-    // K1 writes there itself (in place when want == d)
-    T* other = (want == d) ? tmp : d;
-    T* cur = (passes % 2 == 0) ? want : other;
+    // buffer written by step k (0 = the first kernel, k = pass k): out for the
+    // last, then wa, wb, wa, ... going backwards
+    auto written_by = [&](int k) -> T* { return k == passes ? out : (((passes - k) & 1) ? wa : wb); };
+    T* cur = written_by(0);
     int64_t* splits = static_cast<int64_t*>(scratch);
     int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
                                       pipeline_scratch_bytes<T>(n, sort_n, fan) - 256);
@@ -177,7 +184,7 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
-        cudaFuncSetAttribute(range_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
         configured = true;
     }
@@ -191,10 +198,10 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
     launch(n_k1.c_str(), st, [&] {
         if constexpr (C::WARP_K1)
             warp_block_sort_kernel<T, C::K1_NW, C::K1_VT><<<(unsigned)tiles1, C::K1_NW * 32, k1_smem<T>(), st>>>(
-                d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
+                in, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
         else
             block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
-                d, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
+                in, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
     });
     if (stats) {
         stats->kernels++;
@@ -202,7 +209,7 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
     }
     for (int pi = 0; pi < passes; ++pi) {
         const PassPlan& p = plan[pi];
-        T* nxt = (cur == want) ? other : want;
+        T* nxt = written_by(pi + 1);
         const uint64_t xo = pi + 1 == passes ? key_mask : 0;
         if (p.fan == 2) {
             const uint64_t tiles = (n + MT - 1) / MT;
@@ -219,14 +226,14 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
         } else {
             if (p.rpg > 1) {
                 launch(n_ks.c_str(), st, [&] {
-                    kway_split_kernel<T><<<(unsigned)(p.groups * (p.rpg + 1)), 256, 0, st>>>(
-                        cur, n, p.run, p.fan, p.rpg, splits, err);
+                    kway_split_kernel<T, RunLists<T>><<<(unsigned)(p.groups * (p.rpg + 1)), 256, 0, st>>>(
+                        RunLists<T>{cur, n, p.run, p.fan}, p.rpg, 0, splits, err);
                 });
                 if (stats) stats->kernels++;
             }
             launch(n_km.c_str(), st, [&] {
-                range_merge_kernel<T><<<(unsigned)(p.groups * p.rpg), KC::NT, KwayLayout<T>::SMEM, st>>>(
-                    cur, nxt, n, p.run, p.fan, p.rpg, p.rpg > 1 ? splits : nullptr, xo);
+                range_merge_kernel<T, RunLists<T>><<<(unsigned)(p.groups * p.rpg), KC::NT, KwayLayout<T>::SMEM, st>>>(
+                    RunLists<T>{cur, n, p.run, p.fan}, nxt, p.rpg, p.rpg > 1 ? splits : nullptr, 0, xo);
             });
             if (stats) stats->kernels++;
         }
@@ -234,6 +241,17 @@ cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
         cur = nxt;
     }
     return cudaGetLastError();
+}
+
+// Sorts d[0..n) in chunks of sort_n into `want` (d or tmp), ping-ponging
+// between the two: the last pass writes want, so the one before writes the
+// other buffer. With an even number of merge passes the first kernel writes
+// want itself (in place when want == d).
+template <class T>
+cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, T* want,
+                          int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
+    T* other = (want == d) ? tmp : d;
+    return sort_pipeline_io<T>(d, want, other, want, n, sort_n, key_mask, fan, scratch, st, stats);
 }
 
 }  // namespace origami

@@ -11,6 +11,12 @@ cudaError_t sort_kv(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
                               static_cast<KV64*>(want), fan, scratch, st, stats);
 }
 
+cudaError_t sort_io_kv(const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n,
+                        uint64_t key_mask, int fan, void* scratch, cudaStream_t st) {
+    return sort_pipeline_io<KV64>(static_cast<const KV64*>(in), static_cast<KV64*>(out), static_cast<KV64*>(wa),
+                                static_cast<KV64*>(wb), n, sort_n, key_mask, fan, scratch, st, nullptr);
+}
+
 uint64_t scratch_bytes_kv(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<KV64>(n, sort_n, fan);
 }
