@@ -190,6 +190,14 @@ def short_workloads(torch):
     except Exception as e:  # reported in the line
         out["batched"] = {"error": repr(e)}
     try:
+        out["plain_configs"] = wl.plain_configs(torch)
+    except Exception as e:
+        out["plain_configs"] = {"error": repr(e)}
+    try:
+        out["kv_distributions"] = wl.kv_distributions(torch, steps=2, warmup=1)
+    except Exception as e:
+        out["kv_distributions"] = {"error": repr(e)}
+    try:
         sv = wl.serving(torch, rates=(100, 200, 400), duration_s=2.0, pool_size=64)
         out["serving"] = sv
         ok = [r for r in sv["rates"] if r["failed"] == 0]
@@ -209,9 +217,25 @@ def run_workload(args, torch, world, rank):
     if rank != 0:
         return
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    if args.workload == "batched":
-        r = wl.batched(torch, steps=args.steps, warmup=args.warmup, loop_steps=2)
-        line = {"metric": "Gkeys/s batched segmented sort (65,536 uint32 arrays, one graph replay)",
+    if args.workload == "kv":
+        r = wl.kv_distributions(torch, steps=args.steps, warmup=args.warmup)
+        line = {"metric": "Gkeys/s key-value sort of 134,217,728 (uint64, uint64) pairs per distribution",
+                "value": min(x["gkeys_s"] for x in r.values()), "unit": "Gkeys/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "kvu64", "data": "synthetic",
+                "config": {"workload": "2^27 pairs, value = input index; " + ", ".join(wl.KV_DISTS)},
+                "detail": r}
+    elif args.workload == "plain":
+        r = wl.plain_configs(torch, steps=args.steps, warmup=args.warmup)
+        line = {"metric": "Gkeys/s: 1 GiB uint64 sort and 1 GiB uint32 chunked sorts",
+                "value": r["u64_1GiB"]["gkeys_s"], "unit": "Gkeys/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u64/u32", "data": "synthetic", "config": {"workload": "134,217,728 uniform uint64 keys (1 GiB), full sort; 268,435,456 uniform "
+                                                         "uint32 keys (1 GiB) in chunks of 2^17..2^21 keys"}, "detail": r}
+    elif args.workload == "batched":
+        r = wl.batched(torch, steps=args.steps, warmup=args.warmup, nseg=args.segments, hi=args.max_len,
+                       loop_steps=args.loop_steps)
+        line = {"metric": f"Gkeys/s batched segmented sort ({args.segments} uint32 arrays, one graph replay)",
                 "value": r["segmented_gkeys_s"], "unit": "Gkeys/s", "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": r["segmented_graph_ms"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -239,8 +263,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched and serving measurements added to the line")
-    ap.add_argument("--workload", default="sort", choices=["sort", "batched", "serving"],
-                    help="sort: the headline line; batched / serving: that workload alone, in full")
+    ap.add_argument("--workload", default="sort", choices=["sort", "batched", "serving", "kv", "plain"],
+                    help="sort: the headline line; batched / serving / kv / plain: that workload alone")
+    ap.add_argument("--segments", type=int, default=65536, help="batched: number of arrays")
+    ap.add_argument("--max-len", type=int, default=1 << 20, help="batched: longest array")
+    ap.add_argument("--loop-steps", type=int, default=2, help="batched: timed runs of the plain-sort loop")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

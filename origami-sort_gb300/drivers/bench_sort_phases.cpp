@@ -9,7 +9,7 @@
 //   phase2  chunked sorts for sort_n from 32 up to 128K items: the sizes the
 //           reference keeps in L2 (sort_sliding_test, Table 10)
 //   phase3  chunked sorts for sort_n from 256K items up to the whole array
-//           (Table 11), including config 2's chunk sweep 128K..2M
+//           (Table 11), including the chunk sweep 128K..2M of the README
 //   phase4  the full sort at every merge fan-in min_k = 2, 4, 8, 16 (the
 //           switch point between binary and k-way passes; Tables 13-14)
 // Every line gives Mkeys/s, the number of HBM passes (launches of the sort and

@@ -266,3 +266,143 @@ def serving(torch, rates=(100, 200, 400, 800), duration_s=3.0, pool_size=96, see
         dt += time.perf_counter() - t0
     out["loop_plain_keys_per_s"] = pool.keys / dt
     return out
+
+
+# ------------------------------------------------- key-value distributions --
+KV_DISTS = ("uniform", "zipf", "sorted", "reverse", "equal", "runs8")
+
+
+def kv_input(torch, n, dist, gen, dev):
+    """n uint64 keys (int64 storage) of one distribution; values are added by
+    the caller. uniform over [0, 2^64); Zipf(1.0) over 2^20 ranks, key = rank
+    times an odd 64-bit constant; sorted / reverse sorted uniform keys; one
+    seeded value; 8 interleaved ascending runs (item i in run i mod 8)."""
+    def uniform(m):
+        lo = torch.randint(0, 2**32, (m,), dtype=torch.int64, device=dev, generator=gen)
+        hi = torch.randint(0, 2**32, (m,), dtype=torch.int64, device=dev, generator=gen)
+        return (hi << 32) | lo
+
+    def unsigned_sorted(k):  # ascending as uint64: sort the sign-flipped values
+        flip = k ^ (-(2**63))
+        return torch.sort(flip).values ^ (-(2**63))
+
+    if dist == "uniform":
+        return uniform(n)
+    if dist == "zipf":
+        return device_keys(torch, n, gen, dev, zipf=True, words=2).view(torch.int64)
+    if dist == "sorted":
+        return unsigned_sorted(uniform(n))
+    if dist == "reverse":
+        return unsigned_sorted(uniform(n)).flip(0)
+    if dist == "equal":
+        return uniform(1).expand(n).contiguous()
+    if dist == "runs8":
+        m = (n + 7) // 8
+        runs = torch.stack([unsigned_sorted(uniform(m)) for _ in range(8)], dim=1)  # [m, 8]
+        return runs.reshape(-1)[:n].contiguous()
+    raise ValueError(dist)
+
+
+def kv_distributions(torch, n=1 << 27, steps=3, warmup=2, seed=3, dev=None):
+    """Sort n (uint64 key, uint64 value = original index) pairs under every
+    distribution. Checks on the device: keys ascending, and the pairs intact
+    (key[i] == input key[value[i]], values a permutation) with equal keys in
+    input order (stable)."""
+    import ctypes
+    from . import KVU64
+    dev = dev or torch.device("cuda", torch.cuda.current_device())
+    gen = torch.Generator(device=dev).manual_seed(seed)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for dist in KV_DISTS:
+        keys = kv_input(torch, n, dist, gen, dev)
+        pristine = torch.stack([keys, torch.arange(n, device=dev, dtype=torch.int64)], dim=1).contiguous()
+        d = torch.empty_like(pristine)
+        tmp = torch.empty_like(pristine)
+        res = ctypes.c_void_p()
+        L = lib()
+
+        def one():
+            check(L.origami_sort_device(KVU64, d.data_ptr(), tmp.data_ptr(), n, 0, 0, 0, ctypes.byref(res),
+                                        ctypes.c_void_p(stream.cuda_stream)))
+
+        for _ in range(warmup):
+            d.copy_(pristine)
+            one()
+        ms = []
+        for _ in range(steps):
+            d.copy_(pristine)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        k, v = d[:, 0], d[:, 1]
+        flip = k ^ (-(2**63))
+        asc = bool((flip[1:] >= flip[:-1]).all().item())
+        intact = bool((keys[v] == k).all().item())
+        perm = bool((torch.sort(v).values == torch.arange(n, device=dev)).all().item())
+        same = k[1:] == k[:-1]
+        stable = bool(((v[1:] > v[:-1]) | ~same).all().item())
+        t = float(np.mean(ms))
+        out[dist] = {"ms": t, "gkeys_s": n / t / 1e6, "sorted": asc, "pairs_intact": intact and perm,
+                     "stable": stable}
+        del keys, pristine, d, tmp, k, v, flip, same
+        torch.cuda.empty_cache()
+    return out
+
+
+def plain_configs(torch, steps=3, warmup=2, dev=None):
+    """1 GiB as 134,217,728 uniform uint64 keys, and the 1 GiB uint32 array
+    sorted in chunks of 128K..2M keys (device-resident, CUDA events)."""
+    import ctypes
+    from . import U64
+    dev = dev or torch.device("cuda", torch.cuda.current_device())
+    gen = torch.Generator(device=dev).manual_seed(5)
+    stream = torch.cuda.current_stream(dev)
+    L = lib()
+    res = ctypes.c_void_p()
+
+    def timed(kind, pristine, d, tmp, n, sort_n):
+        def one():
+            check(L.origami_sort_device(kind, d.data_ptr(), tmp.data_ptr(), n, sort_n, 0, 0, ctypes.byref(res),
+                                        ctypes.c_void_p(stream.cuda_stream)))
+        for _ in range(warmup):
+            d.copy_(pristine)
+            one()
+        ms = []
+        for _ in range(steps):
+            d.copy_(pristine)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.mean(ms))
+
+    out = {}
+    n64 = 1 << 27
+    p = torch.randint(-(2**63), 2**63 - 1, (n64,), dtype=torch.int64, device=dev, generator=gen)
+    d, tmp = torch.empty_like(p), torch.empty_like(p)
+    t = timed(U64, p, d, tmp, n64, 0)
+    flip = d ^ (-(2**63))
+    out["u64_1GiB"] = {"n": n64, "ms": t, "gkeys_s": n64 / t / 1e6,
+                       "sorted": bool((flip[1:] >= flip[:-1]).all().item())}
+    del p, d, tmp, flip
+    n32 = 1 << 28
+    p = torch.randint(-(2**31), 2**31, (n32,), dtype=torch.int32, device=dev, generator=gen)
+    d, tmp = torch.empty_like(p), torch.empty_like(p)
+    chunks = {}
+    for sh in range(17, 22):
+        s = 1 << sh
+        t = timed(U32, p, d, tmp, n32, s)
+        flip = (d ^ (-(2**31))).view(-1, s)
+        ok = bool((flip[:, 1:] >= flip[:, :-1]).all().item())
+        chunks[str(s)] = {"ms": t, "gkeys_s": n32 / t / 1e6, "sorted_chunks": ok}
+        del flip
+    out["u32_1GiB_chunked"] = chunks
+    del p, d, tmp
+    torch.cuda.empty_cache()
+    return out
