@@ -111,6 +111,40 @@ __device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int i
     }
 }
 
+// merge_block into registers: out[0 .. cnt) receive the block's outputs, so
+// that the caller can overwrite the source buffer once every thread is done
+// reading it.
+template <class T, int VT, bool STABLE>
+__device__ __forceinline__ void merge_block_regs(const T* src, int ia0, int ib0, int na, int cnt, T (&out)[VT]) {
+    const int nb = cnt - na;
+    if constexpr (STABLE) {
+        int ia = ia0, ib = ib0;
+        const int aEnd = ia0 + na, bEnd = ib0 + nb;
+        T x = src[ia];
+        T y = src[ib];
+#pragma unroll
+        for (int i = 0; i < VT; ++i) {
+            if (i < cnt) {
+                const bool takeA = (ib >= bEnd) || (ia < aEnd && !less(y, x));
+                out[i] = takeA ? x : y;
+                const int nxt = takeA ? ++ia : ++ib;
+                const T vv = src[nxt];
+                x = takeA ? vv : x;
+                y = takeA ? y : vv;
+            }
+        }
+    } else {
+        const int pb = ib0 + VT - 1;  // B is read backwards: slot i holds B[pb - i]
+#pragma unroll
+        for (int i = 0; i < VT; ++i) {
+            const bool fromA = i < na;
+            const T t = src[fromA ? ia0 + i : pb - i];
+            out[i] = (fromA || i >= VT - nb) ? t : Traits<T>::max_item();
+        }
+        bitonic_clean<T, VT>(out);
+    }
+}
+
 // Round over pairs of equal width w inside `total` items (the last pair may be
 // short or absent): the tile sort's rounds. `split` is shared scratch of
 // blocks + 1 ints, blocks = ceil(total / VO) + total / (2w) + 1.
@@ -216,6 +250,39 @@ __device__ __forceinline__ void merge_pair_round(const T* src, int as, int na, i
         const int sa = split[blk];
         const int ea = (blk + 1 < nblk) ? split[blk + 1] : na;
         merge_block<T, VT, STABLE, LinIdx>(src, dst, as + sa, bs + (diag - sa), ea - sa, cnt, diag);
+    }
+    __syncthreads();
+}
+
+// merge_pair_round that writes its output over its own input: `buf` holds A
+// at [as, as+na) and B at [bs, bs+nb) and receives the merge at [0, na+nb).
+// Every thread owns at most one block (NT * VO >= na + nb), keeps it in
+// registers while the others read, then stores it. The output may therefore
+// share the input's shared memory, which halves the footprint of a tile.
+template <class T, int NT, int VT, bool STABLE>
+__device__ __forceinline__ void merge_pair_round_inplace(T* buf, int as, int na, int bs, int nb, int* split) {
+    constexpr int VO = Block<T, VT, STABLE>::VO;
+    const int tid = threadIdx.x;
+    const int total = na + nb;
+    const int nblk = (total + VO - 1) / VO;
+    if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, as, na, bs, nb, tid * VO);
+    __syncthreads();
+    T r[VT];
+    const int diag = tid * VO;
+    const int cnt = tid < nblk ? min(VO, total - diag) : 0;
+    if (tid < nblk) {
+        const int sa = split[tid];
+        const int ea = (tid + 1 < nblk) ? split[tid + 1] : na;
+        merge_block_regs<T, VT, STABLE>(buf, as + sa, bs + (diag - sa), ea - sa, cnt, r);
+    }
+    __syncthreads();
+    if (cnt == VO) {
+#pragma unroll
+        for (int i = 0; i < VO; ++i) buf[diag + i] = r[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < VO; ++i)
+            if (i < cnt) buf[diag + i] = r[i];
     }
     __syncthreads();
 }

@@ -224,14 +224,14 @@ __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uin
 // and the tile is written back coalesced.
 template <class T, int NT, int VT, bool STABLE, int TILE>
 struct PairShape {
-    // input: A part and B part each padded to whole 16-byte vectors (+ read slack)
+    // input: A part and B part each padded to whole 16-byte vectors (+ read
+    // slack); the merged tile is written back over the same buffer
     static constexpr int V = Vec<T>::N;
     static constexpr int IN_CAP = TILE + 4 * V + VT + 4;
-    static constexpr int OUT_CAP = TILE + 4;
     static constexpr size_t IN_BYTES = (((size_t)IN_CAP * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr size_t OUT_BYTES = (((size_t)OUT_CAP * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr size_t SMEM = IN_BYTES + OUT_BYTES;
+    static constexpr size_t SMEM = IN_BYTES;
     static constexpr int SPLITS = TILE / Block<T, VT, STABLE>::VO + 4;
+    static_assert(NT * Block<T, VT, STABLE>::VO >= TILE, "one merge block per thread");
 };
 
 template <class T, int NT, int VT, bool STABLE, int TILE>
@@ -243,7 +243,6 @@ __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ sr
     constexpr int V = Sh::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sin = reinterpret_cast<T*>(smem_raw);
-    T* sout = reinterpret_cast<T*>(smem_raw + Sh::IN_BYTES);
     __shared__ int split[Sh::SPLITS];
     const int tid = threadIdx.x;
     const uint64_t t = blockIdx.x;
@@ -266,7 +265,8 @@ __global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ sr
     cp_async_commit_all();
     cp_async_wait_all();
     __syncthreads();
-    merge_pair_round<T, NT, VT, STABLE>(sin, a_lead, na, b_base + b_lead, nb, sout, split);
+    merge_pair_round_inplace<T, NT, VT, STABLE>(sin, a_lead, na, b_base + b_lead, nb, split);
+    const T* sout = sin;
     // output tile starts 16-byte aligned (o is a multiple of TILE)
     T* out = dst + o;
     const int nvec = total / V;
