@@ -24,32 +24,33 @@ template <>
 struct Config<uint32_t> {
     // K1: warps sort 32*32 keys in registers, then shared-memory rounds to 8192
     static constexpr bool WARP_K1 = true;
-    static constexpr int K1_NW = 8, K1_VT = 32;
+    // 8 warps sort 1024 keys each; 9 warps share the merge rounds (265 blocks)
+    static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 32, K1_MINB = 3;
     static constexpr int K1_NT = 256, K1_VTS = 32, K1_VTM = 32;  // (block K1, unused)
-    static constexpr int P_NT = 288, P_VT = 32, P_TILE = 8192;    // binary pass tiles
+    static constexpr int P_NT = 160, P_VT = 32, P_TILE = 4096, P_MINB = 1;  // binary pass tiles
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<uint64_t> {
     static constexpr bool WARP_K1 = true;
-    static constexpr int K1_NW = 8, K1_VT = 16;
+    static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 1;
     static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
-    static constexpr int P_NT = 288, P_VT = 16, P_TILE = 4096;
+    static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 8;
     static constexpr bool STABLE = false;
 };
 template <>
 struct Config<KV64> {
     static constexpr bool WARP_K1 = false;  // key-value items need stable merges
-    static constexpr int K1_NW = 8, K1_VT = 8;
+    static constexpr int K1_NW = 8, K1_NWT = 8, K1_VT = 8, K1_MINB = 1;
     static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 7;  // 2048 items (32 KiB)
-    static constexpr int P_NT = 320, P_VT = 7, P_TILE = 2048;
+    static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 1;  // serial merge blocks of 11
     static constexpr bool STABLE = true;
 };
 
 template <class T>
 using K1Shape = BlockSortShape<T, Config<T>::K1_NT, Config<T>::K1_VTS, Config<T>::K1_VTM, Config<T>::STABLE>;
 template <class T>
-using K1WShape = WarpSortShape<T, Config<T>::K1_NW, Config<T>::K1_VT>;
+using K1WShape = WarpSortShape<T, Config<T>::K1_NW, Config<T>::K1_VT, Config<T>::K1_NWT>;
 template <class T>
 constexpr int k1_tile() {
     return Config<T>::WARP_K1 ? K1WShape<T>::TILE : K1Shape<T>::TILE;
@@ -177,12 +178,12 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     static bool configured = false;
     if (!configured) {
         if constexpr (C::WARP_K1)
-            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT>,
+            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         else
             cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
-        cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE>,
+        cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
@@ -197,7 +198,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     const uint64_t tiles1 = (n + T1 - 1) / T1;
     launch(n_k1.c_str(), st, [&] {
         if constexpr (C::WARP_K1)
-            warp_block_sort_kernel<T, C::K1_NW, C::K1_VT><<<(unsigned)tiles1, C::K1_NW * 32, k1_smem<T>(), st>>>(
+            warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB><<<(unsigned)tiles1, C::K1_NWT * 32,
+                                                                                   k1_smem<T>(), st>>>(
                 in, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
         else
             block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
@@ -219,7 +221,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                 pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
             });
             launch(n_k3.c_str(), st, [&] {
-                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE><<<(unsigned)tiles, C::P_NT, merge_smem<T>(), st>>>(
+                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB><<<(unsigned)tiles, C::P_NT,
+                                                                                         merge_smem<T>(), st>>>(
                     cur, nxt, n, run, splits, xo);
             });
             if (stats) stats->kernels += 2;

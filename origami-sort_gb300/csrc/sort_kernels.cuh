@@ -86,12 +86,15 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
     }
 }
 
-// K1 for keys-only items: every warp sorts 32*VT keys entirely in registers
-// (lane network + shuffle merges, warp_sort.cuh), then merge rounds in shared
-// memory join the warps' runs into a tile of NW*32*VT keys.
-template <class T, int NW, int VT>
+// K1 for keys-only items: every one of NW warps sorts 32*VT keys entirely in
+// registers (lane network + shuffle merges, warp_sort.cuh), then merge rounds
+// in shared memory join the warps' runs into a tile of NW*32*VT keys. NWT >= NW
+// warps share the merge rounds, so that every thread owns at most one merge
+// block per round (NWT*32*(VT-1) >= tile).
+template <class T, int NW, int VT, int NWT = NW>
 struct WarpSortShape {
     static constexpr int NT = NW * 32;
+    static constexpr int NTM = NWT * 32;
     static constexpr int TILE = NT * VT;
     static constexpr int WTILE = 32 * VT;
     static constexpr int BUF = padded_items<T>(TILE + VT + 1);
@@ -100,12 +103,13 @@ struct WarpSortShape {
     static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
 };
 
-template <class T, int NW, int VT>
-__global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __restrict__ in,
-                                                                 T* __restrict__ out, uint64_t n,
-                                                                 int chunk, uint64_t xin,
-                                                                 uint64_t xout) {
-    using Sh = WarpSortShape<T, NW, VT>;
+template <class T, int NW, int VT, int NWT = NW, int MINB = 1>
+__global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T* __restrict__ in,
+                                                                        T* __restrict__ out, uint64_t n,
+                                                                        int chunk, uint64_t xin,
+                                                                        uint64_t xout) {
+    using Sh = WarpSortShape<T, NW, VT, NWT>;
+    static_assert(NWT >= NW, "the sorting warps take part in the merge rounds");
     constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sa = reinterpret_cast<T*>(smem_raw);
@@ -118,46 +122,51 @@ __global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __res
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const int w0 = warp * WT;
 
-    // each lane loads its VT consecutive keys with 16-byte vector loads
-    // (blocked order; a partial tail is filled with the largest key)
+    // each lane loads VT keys with 16-byte vector loads; a partial tail is
+    // filled with the largest key. When a chunk spans the warp's whole run the
+    // lanes' keys may come from anywhere in it, so the loads are striped
+    // (each instruction reads 512 contiguous bytes); smaller chunks need each
+    // lane to hold its own VT consecutive keys (blocked).
     constexpr int V = Vec<T>::N;
     T v[VT];
-    {
-        const int i0 = w0 + lane * VT;
-        const T* src = in + base + i0;
+    const bool sorter = warp < NW;
+    if (sorter) {
+        const bool striped = chunk >= WT;
 #pragma unroll
         for (int j = 0; j < VT / V; ++j) {
-            if (i0 + (j + 1) * V <= valid) {
-                const uint4 q = *reinterpret_cast<const uint4*>(src + j * V);
+            const int i0 = striped ? w0 + j * 32 * V + lane * V : w0 + lane * VT + j * V;
+            const T* src = in + base + i0;
+            if (i0 + V <= valid) {
+                const uint4 q = *reinterpret_cast<const uint4*>(src);
                 const T* e = reinterpret_cast<const T*>(&q);
 #pragma unroll
                 for (int k = 0; k < V; ++k) v[j * V + k] = Traits<T>::flip(e[k], xin);
             } else {
 #pragma unroll
-                for (int k = 0; k < V; ++k) {
-                    const int i = i0 + j * V + k;
-                    v[j * V + k] = (i < valid) ? Traits<T>::flip(src[j * V + k], xin) : Traits<T>::max_item();
-                }
+                for (int k = 0; k < V; ++k)
+                    v[j * V + k] = (i0 + k < valid) ? Traits<T>::flip(src[k], xin) : Traits<T>::max_item();
             }
         }
+        warp_sort<T, VT>(v, chunk);
     }
-    warp_sort<T, VT>(v, chunk);
     if (WT < TILE && WT < chunk) {
+        if (sorter) {
 #pragma unroll
-        for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+            for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+        }
         __syncthreads();
-        merge_round_uniform<T, Sh::NT, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
+        merge_round_uniform<T, Sh::NTM, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
         T* src = sb;
         T* dst = sa;
         for (int w = 2 * WT; w < TILE && w < chunk; w <<= 1) {
-            merge_round_uniform<T, Sh::NT, VT, false, LinIdx>(src, dst, w, TILE, split);
+            merge_round_uniform<T, Sh::NTM, VT, false, LinIdx>(src, dst, w, TILE, split);
             T* t = src;
             src = dst;
             dst = t;
         }
         // coalesced 16-byte stores of the sorted tile
         const int nvec = valid / V;
-        for (int i = tid; i < nvec; i += Sh::NT) {
+        for (int i = tid; i < nvec; i += Sh::NTM) {
             const uint4 q = *reinterpret_cast<const uint4*>(src + (size_t)i * V);
             T e[V];
             const T* qe = reinterpret_cast<const T*>(&q);
@@ -165,8 +174,8 @@ __global__ void __launch_bounds__(NW * 32) warp_block_sort_kernel(const T* __res
             for (int k = 0; k < V; ++k) e[k] = Traits<T>::flip(qe[k], xout);
             *reinterpret_cast<uint4*>(out + base + (size_t)i * V) = *reinterpret_cast<const uint4*>(e);
         }
-        for (int i = nvec * V + tid; i < valid; i += Sh::NT) out[base + i] = Traits<T>::flip(src[i], xout);
-    } else {
+        for (int i = nvec * V + tid; i < valid; i += Sh::NTM) out[base + i] = Traits<T>::flip(src[i], xout);
+    } else if (sorter) {
         // runs end at the warp (or chunk) size: each lane stores its own keys
         const int i0 = w0 + lane * VT;
         T* dp = out + base + i0;
@@ -234,8 +243,8 @@ struct PairShape {
     static_assert(NT * Block<T, VT, STABLE>::VO >= TILE, "one merge block per thread");
 };
 
-template <class T, int NT, int VT, bool STABLE, int TILE>
-__global__ void __launch_bounds__(NT) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
+template <class T, int NT, int VT, bool STABLE, int TILE, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                         uint64_t n, uint64_t run,
                                                         const int64_t* __restrict__ splits,
                                                         uint64_t xout) {
