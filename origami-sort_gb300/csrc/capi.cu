@@ -285,37 +285,121 @@ void* device_view(void* p) {
     return nullptr;
 }
 
-int typed_io(int kind, const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n, int fan,
-             void* scratch, cudaStream_t st) {
-    const uint64_t m = key_mask(kind);
-    cudaError_t e;
+cudaError_t typed_io(int kind, const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n,
+                     uint64_t xin, uint64_t xout, uint64_t start_run, int fan, void* scratch, cudaStream_t st) {
     switch (kind) {
-        case ORIGAMI_U32: e = sort_io_u32(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
+        case ORIGAMI_U32: return sort_io_u32(in, out, wa, wb, n, sort_n, xin, xout, start_run, fan, scratch, st);
         case ORIGAMI_U64:
-        case ORIGAMI_I64: e = sort_io_u64(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
-        default: e = sort_io_kv(in, out, wa, wb, n, sort_n, m, fan, scratch, st); break;
+        case ORIGAMI_I64: return sort_io_u64(in, out, wa, wb, n, sort_n, xin, xout, start_run, fan, scratch, st);
+        default: return sort_io_kv(in, out, wa, wb, n, sort_n, xin, xout, start_run, fan, scratch, st);
     }
-    return e == cudaSuccess ? ORIGAMI_OK : cuda_fail(e, "sort launch");
 }
 
-// Host buffers the device can address: the first kernel reads them over the
-// host link and the last pass writes the result straight back, so no copy
-// pass is made; the merge passes in between use two arena buffers.
-int sort_host_direct(int kind, const void* vin, void* vout, uint64_t n, uint64_t sort_n, unsigned min_k,
-                     cudaStream_t st) {
-    const uint64_t bytes = n * item_bytes(kind);
+uint64_t typed_scratch_io(int kind, uint64_t n, uint64_t sort_n, int fan, uint64_t start_run) {
+    switch (kind) {
+        case ORIGAMI_U32: return scratch_bytes_io_u32(n, sort_n, fan, start_run);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return scratch_bytes_io_u64(n, sort_n, fan, start_run);
+        default: return scratch_bytes_io_kv(n, sort_n, fan, start_run);
+    }
+}
+
+// Second compute stream and copy stream of the calling thread (host sorts).
+cudaStream_t aux_stream(int which) {
+    thread_local cudaStream_t s[2] = {nullptr, nullptr};
+    if (!s[which]) cudaStreamCreateWithFlags(&s[which], cudaStreamNonBlocking);
+    return s[which];
+}
+
+bool is_pinned(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Host buffers the device can address (view pointers vin / vout).
+//  * Small sorts, fan-in > 2, or chunk sizes of at most one chunk: one
+//    pipeline whose first kernel reads the host input and whose last pass
+//    writes the host output, with the passes in between in two arena buffers.
+//  * Large sorts: the input is cut into chunks of chunk_n (a power of two,
+//    about n/8). Each chunk arrives in HBM (a copy-engine transfer for pinned
+//    memory, else the first kernel's own reads) and is sorted on one of two
+//    compute streams while the next chunk is in flight; the merge passes
+//    across chunks follow, the last of them writing the host output. The host
+//    link then carries each byte once each way, overlapped with the chunk sorts.
+int sort_host_direct(int kind, void* host_in, const void* vin, void* vout, uint64_t n, uint64_t sort_n,
+                     unsigned min_k, cudaStream_t st) {
+    const uint64_t ib = item_bytes(kind);
+    const uint64_t bytes = n * ib;
     const int fan = fan_of(min_k);
-    void *wa = nullptr, *wb = nullptr, *work = nullptr;
-    CK(cudaMallocAsync(&wa, bytes, st), "arena allocation");
-    cudaError_t e = cudaMallocAsync(&wb, bytes, st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&work, scratch_bytes(kind, n, sort_n, fan), st);
-    int rc = e == cudaSuccess ? typed_io(kind, vin, vout, wa, wb, n, sort_n, fan, work, st)
-                              : cuda_fail(e, "arena allocation");
-    if (work) cudaFreeAsync(work, st);
-    if (wb) cudaFreeAsync(wb, st);
-    cudaFreeAsync(wa, st);
+    const uint64_t m = key_mask(kind);
+    const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
+    uint64_t chunk_n = 1ull << 22;
+    while (chunk_n * 16 <= n) chunk_n <<= 1;  // 8 to 16 chunks
+    const bool chunked = fan == 2 && n >= 4 * chunk_n && limit > chunk_n;
+    void *A = nullptr, *B = nullptr, *w0 = nullptr, *w1 = nullptr, *wm = nullptr;
+    CK(cudaMallocAsync(&A, bytes, st), "arena allocation");
+    cudaError_t e = cudaMallocAsync(&B, bytes, st);
+    if (!chunked) {
+        if (e == cudaSuccess) e = cudaMallocAsync(&w0, typed_scratch_io(kind, n, sort_n, fan, 0), st);
+        if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w0, st);
+    } else {
+        const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, fan, 0);
+        if (e == cudaSuccess) e = cudaMallocAsync(&w0, cs, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&w1, cs, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&wm, typed_scratch_io(kind, n, sort_n, fan, chunk_n), st);
+        const bool copy_in = is_pinned(host_in);
+        cudaStream_t s1 = aux_stream(0), sc = aux_stream(1);
+        std::vector<cudaEvent_t> evs;
+        auto event_on = [&](cudaStream_t s) {
+            cudaEvent_t ev;
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            cudaEventRecord(ev, s);
+            evs.push_back(ev);
+            return ev;
+        };
+        if (e == cudaSuccess) {
+            const cudaEvent_t ready = event_on(st);  // buffers allocated
+            cudaStreamWaitEvent(s1, ready, 0);
+            cudaStreamWaitEvent(sc, ready, 0);
+        }
+        char* a = static_cast<char*>(A);
+        char* b = static_cast<char*>(B);
+        for (uint64_t off = 0, c = 0; e == cudaSuccess && off < n; off += chunk_n, ++c) {
+            const uint64_t cn = n - off < chunk_n ? n - off : chunk_n;
+            cudaStream_t cst = (c & 1) ? s1 : st;
+            const void* src = static_cast<const char*>(vin) + off * ib;
+            if (copy_in) {
+                e = cudaMemcpyAsync(a + off * ib, static_cast<const char*>(host_in) + off * ib, cn * ib,
+                                    cudaMemcpyHostToDevice, sc);
+                cudaStreamWaitEvent(cst, event_on(sc), 0);
+                src = a + off * ib;
+            }
+            if (e == cudaSuccess)
+                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, fan,
+                             (c & 1) ? w1 : w0, cst);
+        }
+        if (e == cudaSuccess) {
+            cudaStreamWaitEvent(st, event_on(s1), 0);
+            // merges from runs of chunk_n: the first pass must not write A, which it reads
+            int passes = 0;
+            for (uint64_t r = chunk_n; r < limit; r <<= 1) ++passes;
+            void* wa = ((passes - 1) & 1) ? B : A;
+            void* wb = ((passes - 1) & 1) ? A : B;
+            e = typed_io(kind, A, vout, wa, wb, n, sort_n, 0, m, chunk_n, fan, wm, st);
+        }
+        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once their work completes
+    }
+    if (wm) cudaFreeAsync(wm, st);
+    if (w1) cudaFreeAsync(w1, st);
+    if (w0) cudaFreeAsync(w0, st);
+    if (B) cudaFreeAsync(B, st);
+    cudaFreeAsync(A, st);
     const cudaError_t es = cudaStreamSynchronize(st);
-    if (rc != ORIGAMI_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "host sort");
     if (es != cudaSuccess) return cuda_fail(es, "stream sync");
     return ORIGAMI_OK;
 }
@@ -335,7 +419,7 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
         void* vin = device_view(d);
         void* vout = vin ? device_view(out) : nullptr;
         if (vin && vout && !((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
-            return sort_host_direct(kind, vin, vout, n, sort_n, min_k, st);
+            return sort_host_direct(kind, d, vin, vout, n, sort_n, min_k, st);
     }
     void* dd = nullptr;
     void* dt = nullptr;

@@ -16,7 +16,10 @@ struct LaunchStats;
                             LaunchStats* stats);                                                \
     uint64_t scratch_bytes_##name(uint64_t n, uint64_t sort_n, int fan);                          \
     cudaError_t sort_io_##name(const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n, \
-                               uint64_t key_mask, int fan, void* scratch, cudaStream_t st);
+                               uint64_t xin, uint64_t xout, uint64_t start_run, int fan, void* scratch,   \
+                               cudaStream_t st);                                                          \
+    uint64_t scratch_bytes_io_##name(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run);          \
+    uint64_t tile_##name();
 ORIGAMI_DECLARE_SORT(u32)
 ORIGAMI_DECLARE_SORT(u64)
 ORIGAMI_DECLARE_SORT(kv)

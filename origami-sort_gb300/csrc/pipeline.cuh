@@ -106,9 +106,9 @@ inline int next_pow2_int(uint64_t v) {
 // fan == 2 gives the binary pipeline; fan in {4, 8, 16} the k-way one, whose
 // last pass uses the smallest fan-in that still reaches `limit`.
 template <class T>
-std::vector<PassPlan> plan_passes(uint64_t n, uint64_t limit, int fan) {
+std::vector<PassPlan> plan_passes(uint64_t n, uint64_t limit, int fan, uint64_t start_run = 0) {
     std::vector<PassPlan> v;
-    uint64_t run = k1_tile<T>();
+    uint64_t run = start_run ? start_run : k1_tile<T>();
     while (run < limit) {
         PassPlan p{run, 2, 0, 1};
         if (fan > 2) {
@@ -133,9 +133,9 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
 // Device scratch (bytes) one sort needs: binary splits or k-way range bounds,
 // plus an error word.
 template <class T>
-uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan) {
+uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run = 0) {
     uint64_t bytes = merge_split_slots<T>(n) * sizeof(int64_t);
-    for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), fan)) {
+    for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), fan, start_run)) {
         if (p.fan > 2 && p.rpg > 1) {
             const uint64_t b = p.groups * (uint64_t)(p.rpg + 1) * KWAY_MAX * sizeof(int64_t);
             bytes = b > bytes ? b : bytes;
@@ -152,11 +152,17 @@ uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan) {
 // in and out may also be host memory the device can address (pinned or, with
 // address translation services, pageable), which streams the data over the
 // host link inside the first and last kernels instead of separate copies.
-// `key_mask` is XORed into every key on the way in and on the way out.
-// `scratch` holds pipeline_scratch_bytes<T>(n, sort_n, fan) bytes of device memory.
+// xin is XORed into every key as the first kernel reads it, xout as the last
+// kernel writes it (the sign flip of signed keys; see common.cuh).
+// start_run > 0 skips the first kernel: `in` already holds sorted runs of
+// start_run items (a multiple of the tile, keys already flipped by xin), and
+// only the merge passes from there to the chunk size run (at least one).
+// `scratch` holds pipeline_scratch_bytes<T>(n, sort_n, fan, start_run) bytes of
+// device memory.
 template <class T>
-cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint64_t sort_n, uint64_t key_mask,
-                             int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
+cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint64_t sort_n, uint64_t xin,
+                             uint64_t xout, uint64_t start_run, int fan, void* scratch, cudaStream_t st,
+                             LaunchStats* stats) {
     using C = Config<T>;
     using KC = KwayCfg<T>;
     constexpr int T1 = k1_tile<T>();
@@ -164,16 +170,17 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     if (n == 0) return cudaSuccess;
     const bool full = (sort_n == 0 || sort_n >= n);
     const uint64_t limit = chunk_limit(n, sort_n);
-    const std::vector<PassPlan> plan = plan_passes<T>(n, limit, fan);
+    const std::vector<PassPlan> plan = plan_passes<T>(n, limit, fan, start_run);
     const int passes = (int)plan.size();
+    if (start_run && passes == 0) return cudaErrorInvalidValue;
     const int k1_chunk = (int)(limit < (uint64_t)T1 ? (full ? T1 : limit) : T1);
     // buffer written by step k (0 = the first kernel, k = pass k): out for the
     // last, then wa, wb, wa, ... going backwards
     auto written_by = [&](int k) -> T* { return k == passes ? out : (((passes - k) & 1) ? wa : wb); };
-    T* cur = written_by(0);
+    const T* cur = start_run ? in : written_by(0);
     int64_t* splits = static_cast<int64_t*>(scratch);
     int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
-                                      pipeline_scratch_bytes<T>(n, sort_n, fan) - 256);
+                                      pipeline_scratch_bytes<T>(n, sort_n, fan, start_run) - 256);
 
     static bool configured = false;
     if (!configured) {
@@ -196,23 +203,27 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
-    launch(n_k1.c_str(), st, [&] {
-        if constexpr (C::WARP_K1)
-            warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB><<<(unsigned)tiles1, C::K1_NWT * 32,
-                                                                                   k1_smem<T>(), st>>>(
-                in, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
-        else
-            block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE><<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(
-                in, cur, n, k1_chunk, key_mask, passes == 0 ? key_mask : 0);
-    });
-    if (stats) {
-        stats->kernels++;
-        stats->passes++;
+    if (!start_run) {
+        T* k1_out = written_by(0);
+        launch(n_k1.c_str(), st, [&] {
+            if constexpr (C::WARP_K1)
+                warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
+                    <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
+                                                                             passes == 0 ? xout : 0);
+            else
+                block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>
+                    <<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
+                                                                       passes == 0 ? xout : 0);
+        });
+        if (stats) {
+            stats->kernels++;
+            stats->passes++;
+        }
     }
     for (int pi = 0; pi < passes; ++pi) {
         const PassPlan& p = plan[pi];
         T* nxt = written_by(pi + 1);
-        const uint64_t xo = pi + 1 == passes ? key_mask : 0;
+        const uint64_t xo = pi + 1 == passes ? xout : 0;
         if (p.fan == 2) {
             const uint64_t tiles = (n + MT - 1) / MT;
             const unsigned pblocks = (unsigned)((tiles + 1 + 255) / 256);
@@ -254,7 +265,7 @@ template <class T>
 cudaError_t sort_pipeline(T* d, T* tmp, uint64_t n, uint64_t sort_n, uint64_t key_mask, T* want,
                           int fan, void* scratch, cudaStream_t st, LaunchStats* stats) {
     T* other = (want == d) ? tmp : d;
-    return sort_pipeline_io<T>(d, want, other, want, n, sort_n, key_mask, fan, scratch, st, stats);
+    return sort_pipeline_io<T>(d, want, other, want, n, sort_n, key_mask, key_mask, 0, fan, scratch, st, stats);
 }
 
 }  // namespace origami

@@ -210,7 +210,9 @@ struct PairGeom {
 
 // ---------------------------------------------------------------- K4 -----
 // One thread per output-tile boundary: the merge-path split (items taken from
-// the left run) at the tile's first output. splits has num_tiles+1 entries.
+// the left run) at the tile's first output, by binary search. (Searches with
+// more probes per step, by one thread or a whole warp, issue more random
+// loads and measured slower.) splits has num_tiles+1 entries.
 template <class T>
 __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uint64_t run, int tile,
                                       uint64_t num_tiles, int64_t* __restrict__ splits) {

@@ -12,10 +12,16 @@ cudaError_t sort_kv(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t ke
 }
 
 cudaError_t sort_io_kv(const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n,
-                        uint64_t key_mask, int fan, void* scratch, cudaStream_t st) {
+                        uint64_t xin, uint64_t xout, uint64_t start_run, int fan, void* scratch, cudaStream_t st) {
     return sort_pipeline_io<KV64>(static_cast<const KV64*>(in), static_cast<KV64*>(out), static_cast<KV64*>(wa),
-                                static_cast<KV64*>(wb), n, sort_n, key_mask, fan, scratch, st, nullptr);
+                                static_cast<KV64*>(wb), n, sort_n, xin, xout, start_run, fan, scratch, st, nullptr);
 }
+
+uint64_t scratch_bytes_io_kv(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run) {
+    return pipeline_scratch_bytes<KV64>(n, sort_n, fan, start_run);
+}
+
+uint64_t tile_kv() { return k1_tile<KV64>(); }
 
 uint64_t scratch_bytes_kv(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<KV64>(n, sort_n, fan);

@@ -12,10 +12,16 @@ cudaError_t sort_u32(void* d, void* tmp, uint64_t n, uint64_t sort_n, uint64_t k
 }
 
 cudaError_t sort_io_u32(const void* in, void* out, void* wa, void* wb, uint64_t n, uint64_t sort_n,
-                        uint64_t key_mask, int fan, void* scratch, cudaStream_t st) {
+                        uint64_t xin, uint64_t xout, uint64_t start_run, int fan, void* scratch, cudaStream_t st) {
     return sort_pipeline_io<uint32_t>(static_cast<const uint32_t*>(in), static_cast<uint32_t*>(out), static_cast<uint32_t*>(wa),
-                                static_cast<uint32_t*>(wb), n, sort_n, key_mask, fan, scratch, st, nullptr);
+                                static_cast<uint32_t*>(wb), n, sort_n, xin, xout, start_run, fan, scratch, st, nullptr);
 }
+
+uint64_t scratch_bytes_io_u32(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run) {
+    return pipeline_scratch_bytes<uint32_t>(n, sort_n, fan, start_run);
+}
+
+uint64_t tile_u32() { return k1_tile<uint32_t>(); }
 
 uint64_t scratch_bytes_u32(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint32_t>(n, sort_n, fan);

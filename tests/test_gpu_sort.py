@@ -174,6 +174,26 @@ def test_pinned_host_buffers():
     assert np.array_equal(r, np.sort(a))
 
 
+@pytest.mark.parametrize("kind,n,pinned,sort_n", [
+    (og.U32, (1 << 24) + 12345, False, 0),
+    (og.U32, 1 << 25, True, 0),
+    (og.I64, (1 << 24) + 7, True, 0),
+    (og.KV64, (1 << 24) + 3, False, 0),
+    (og.U64, 1 << 24, True, 1 << 23),
+    (og.KVU64, 1 << 24, True, 1 << 23),
+])
+def test_host_chunked_pipeline(kind, n, pinned, sort_n):
+    """Large host sorts: chunks sorted while the next ones arrive, then merged,
+    the last pass writing the host buffer (pinned and pageable memory)."""
+    a = make(kind, n, "uniform", seed=11)
+    d = og.empty_host(kind, n, pinned=pinned) if pinned else orc.empty(kind, n)
+    d[:] = a
+    t = og.empty_host(kind, n, pinned=pinned) if pinned else orc.empty(kind, n)
+    r = og.sort(d, t, sort_n=sort_n)
+    assert r is d
+    assert np.array_equal(d, expected(a, sort_n))
+
+
 def _golden_cases(variant):
     with open(GOLDEN) as f:
         doc = json.load(f)
