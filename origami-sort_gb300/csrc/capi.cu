@@ -330,8 +330,40 @@ bool is_pinned(const void* p) {
 //    compute streams while the next chunk is in flight; the merge passes
 //    across chunks follow, the last of them writing the host output. The host
 //    link then carries each byte once each way, overlapped with the chunk sorts.
-int sort_host_direct(int kind, void* host_in, const void* vin, void* vout, uint64_t n, uint64_t sort_n,
-                     unsigned min_k, cudaStream_t st) {
+cudaError_t typed_kway_final(int kind, const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
+                             void* scratch, cudaStream_t st, int slices, void (*cb)(void*, uint64_t, uint64_t),
+                             void* ctx) {
+    switch (kind) {
+        case ORIGAMI_U32: return kway_final_u32(in, out, n, run, fan, xout, scratch, st, slices, cb, ctx);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return kway_final_u64(in, out, n, run, fan, xout, scratch, st, slices, cb, ctx);
+        default: return kway_final_kv(in, out, n, run, fan, xout, scratch, st, slices, cb, ctx);
+    }
+}
+
+// Copies each finished slice of the final pass to the host on the copy stream.
+struct SliceCopy {
+    cudaStream_t st, sc;
+    const char* dev;
+    char* host;
+    uint64_t ib;
+    std::vector<cudaEvent_t>* evs;
+    cudaError_t e;
+    static void on(void* p, uint64_t o0, uint64_t o1) {
+        auto* c = static_cast<SliceCopy*>(p);
+        if (c->e != cudaSuccess || o1 <= o0) return;
+        cudaEvent_t ev;
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        cudaEventRecord(ev, c->st);
+        c->evs->push_back(ev);
+        cudaStreamWaitEvent(c->sc, ev, 0);
+        c->e = cudaMemcpyAsync(c->host + o0 * c->ib, c->dev + o0 * c->ib, (o1 - o0) * c->ib, cudaMemcpyDeviceToHost,
+                               c->sc);
+    }
+};
+
+int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n,
+                     uint64_t sort_n, unsigned min_k, cudaStream_t st) {
     const uint64_t ib = item_bytes(kind);
     const uint64_t bytes = n * ib;
     const int fan = fan_of(min_k);
@@ -350,7 +382,12 @@ int sort_host_direct(int kind, void* host_in, const void* vin, void* vout, uint6
         const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, fan, 0);
         if (e == cudaSuccess) e = cudaMallocAsync(&w0, cs, st);
         if (e == cudaSuccess) e = cudaMallocAsync(&w1, cs, st);
-        if (e == cudaSuccess) e = cudaMallocAsync(&wm, typed_scratch_io(kind, n, sort_n, fan, chunk_n), st);
+        // the merges across chunks are one k-way pass: bound by the host link
+        // it writes (1 GiB in ~5.6 ms), which hides its cost per level
+        const uint64_t need = (limit + chunk_n - 1) / chunk_n;
+        int mfan = 2;
+        while ((uint64_t)mfan < need && mfan < 16) mfan <<= 1;
+        if (e == cudaSuccess) e = cudaMallocAsync(&wm, typed_scratch_io(kind, n, sort_n, mfan, chunk_n), st);
         const bool copy_in = is_pinned(host_in);
         cudaStream_t s1 = aux_stream(0), sc = aux_stream(1);
         std::vector<cudaEvent_t> evs;
@@ -384,12 +421,24 @@ int sort_host_direct(int kind, void* host_in, const void* vin, void* vout, uint6
         }
         if (e == cudaSuccess) {
             cudaStreamWaitEvent(st, event_on(s1), 0);
-            // merges from runs of chunk_n: the first pass must not write A, which it reads
-            int passes = 0;
-            for (uint64_t r = chunk_n; r < limit; r <<= 1) ++passes;
-            void* wa = ((passes - 1) & 1) ? B : A;
-            void* wb = ((passes - 1) & 1) ? A : B;
-            e = typed_io(kind, A, vout, wa, wb, n, sort_n, 0, m, chunk_n, fan, wm, st);
+            if (limit == n && is_pinned(host_out)) {
+                // one k-way pass into HBM in 8 slices; each finished slice goes
+                // to the host on the copy stream while the next ones merge
+                SliceCopy sc_ctx{st, sc, static_cast<const char*>(B), static_cast<char*>(host_out), ib, &evs,
+                                 cudaSuccess};
+                e = typed_kway_final(kind, A, B, n, chunk_n, mfan, m, wm, st, 8, &SliceCopy::on, &sc_ctx);
+                if (e == cudaSuccess) e = sc_ctx.e;
+                cudaStreamWaitEvent(st, event_on(sc), 0);  // B is freed on st after the copies
+            } else {
+                // merges from runs of chunk_n (one pass unless more than 16
+                // chunks form a run); a pass must not write A while the first
+                // one reads it; the last pass writes the host buffer directly
+                int passes = 0;
+                for (uint64_t r = chunk_n; r < limit; r *= (uint64_t)mfan) ++passes;
+                void* wa = ((passes - 1) & 1) ? B : A;
+                void* wb = ((passes - 1) & 1) ? A : B;
+                e = typed_io(kind, A, vout, wa, wb, n, sort_n, 0, m, chunk_n, mfan, wm, st);
+            }
         }
         for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once their work completes
     }
@@ -419,7 +468,7 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
         void* vin = device_view(d);
         void* vout = vin ? device_view(out) : nullptr;
         if (vin && vout && !((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
-            return sort_host_direct(kind, d, vin, vout, n, sort_n, min_k, st);
+            return sort_host_direct(kind, d, out, vin, vout, n, sort_n, min_k, st);
     }
     void* dd = nullptr;
     void* dt = nullptr;

@@ -19,7 +19,10 @@ struct LaunchStats;
                                uint64_t xin, uint64_t xout, uint64_t start_run, int fan, void* scratch,   \
                                cudaStream_t st);                                                          \
     uint64_t scratch_bytes_io_##name(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run);          \
-    uint64_t tile_##name();
+    uint64_t tile_##name();                                                                               \
+    cudaError_t kway_final_##name(const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout, \
+                                  void* scratch, cudaStream_t st, int slices,                            \
+                                  void (*on_slice)(void*, uint64_t, uint64_t), void* ctx);
 ORIGAMI_DECLARE_SORT(u32)
 ORIGAMI_DECLARE_SORT(u64)
 ORIGAMI_DECLARE_SORT(kv)

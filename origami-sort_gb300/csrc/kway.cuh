@@ -272,10 +272,12 @@ struct NoProbe {
 // One CTA per range. groups mode (bnd == nullptr): the range is a whole group.
 // xin: sign flip applied to items as they are read (signed keys straight from a
 // caller's buffer); xout: flip applied as they are written.
+// block0 offsets the block index, so that a pass can be launched in slices of
+// consecutive ranges.
 template <class T, class Lists, class C = KwayCfg<T>, class Probe = NoProbe>
 __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     const Lists lists, T* __restrict__ dst, int rpg, const int64_t* __restrict__ bnd, uint64_t xin,
-    uint64_t xout, Probe probe = Probe()) {
+    uint64_t xout, uint32_t block0 = 0, Probe probe = Probe()) {
     static_assert(C::STABLE || !Traits<T>::kStable, "key-value items need the stable merge");
     using Lay = KwayLayout<T, C>;
     using K = typename Traits<T>::Key;
@@ -296,8 +298,9 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     const int tid = threadIdx.x;
 
     // --- range geometry
-    const uint64_t g = bnd ? blockIdx.x / (uint64_t)rpg : blockIdx.x;
-    const int rb = bnd ? (int)(blockIdx.x % (uint64_t)rpg) : 0;
+    const uint64_t bid = (uint64_t)blockIdx.x + block0;
+    const uint64_t g = bnd ? bid / (uint64_t)rpg : bid;
+    const int rb = bnd ? (int)(bid % (uint64_t)rpg) : 0;
     const auto& geo = lists.group(g);
     if (tid < KWAY_MAX) {
         const uint64_t L = geo.len(tid);

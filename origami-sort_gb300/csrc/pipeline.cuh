@@ -257,6 +257,54 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     return cudaGetLastError();
 }
 
+// One k-way pass merging the F runs of `run` items in[0..n) (n <= run * F,
+// one group) into out, launched in `slices` parts by output range so that the
+// caller can start consuming finished output while later parts merge: after
+// each part, on_slice(o0, o1) is called with the output items [o0, o1) it
+// completed (enqueue work after them on `st`). Keys are already in the
+// internal order; xout is applied as they are written.
+// `scratch` holds kway_pass_scratch_bytes<T>(n) bytes.
+template <class T>
+uint64_t kway_pass_scratch_bytes(uint64_t n) {
+    const uint64_t rpg = (n + KwayCfg<T>::RANGE - 1) / KwayCfg<T>::RANGE;
+    return (rpg + 1) * KWAY_MAX * sizeof(int64_t) + 256;
+}
+
+template <class T, class OnSlice>
+cudaError_t kway_pass_sliced(const T* in, T* out, uint64_t n, uint64_t run, int fan, uint64_t xout, void* scratch,
+                             cudaStream_t st, int slices, OnSlice&& on_slice) {
+    using KC = KwayCfg<T>;
+    static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
+    static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)KwayLayout<T>::SMEM);
+        configured = true;
+    }
+    if (n == 0) return cudaSuccess;
+    const uint64_t rpg = (n + KC::RANGE - 1) / KC::RANGE;
+    int64_t* bnd = static_cast<int64_t*>(scratch);
+    int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) + (rpg + 1) * KWAY_MAX * sizeof(int64_t));
+    const RunLists<T> lists{in, n, run, fan};
+    if (rpg > 1)
+        launch(n_ks.c_str(), st, [&] {
+            kway_split_kernel<T, RunLists<T>><<<(unsigned)(rpg + 1), 256, 0, st>>>(lists, (int)rpg, 0, bnd, err);
+        });
+    if (slices < 1) slices = 1;
+    if ((uint64_t)slices > rpg) slices = (int)rpg;
+    for (int sl = 0; sl < slices; ++sl) {
+        const uint64_t b0 = rpg * sl / slices, b1 = rpg * (sl + 1) / slices;
+        launch(n_km.c_str(), st, [&] {
+            range_merge_kernel<T, RunLists<T>><<<(unsigned)(b1 - b0), KC::NT, KwayLayout<T>::SMEM, st>>>(
+                lists, out, (int)rpg, rpg > 1 ? bnd : nullptr, 0, xout, (uint32_t)b0);
+        });
+        // range b starts at output b * n / rpg (kway_split_kernel's boundaries)
+        on_slice((uint64_t)(((unsigned __int128)b0 * n) / rpg), (uint64_t)(((unsigned __int128)b1 * n) / rpg));
+    }
+    return cudaGetLastError();
+}
+
 // Sorts d[0..n) in chunks of sort_n into `want` (d or tmp), ping-ponging
 // between the two: the last pass writes want, so the one before writes the
 // other buffer. With an even number of merge passes the first kernel writes

@@ -23,6 +23,13 @@ uint64_t scratch_bytes_io_kv(uint64_t n, uint64_t sort_n, int fan, uint64_t star
 
 uint64_t tile_kv() { return k1_tile<KV64>(); }
 
+cudaError_t kway_final_kv(const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
+                          void* scratch, cudaStream_t st, int slices, void (*on_slice)(void*, uint64_t, uint64_t),
+                          void* ctx) {
+    return kway_pass_sliced<KV64>(static_cast<const KV64*>(in), static_cast<KV64*>(out), n, run, fan, xout, scratch, st,
+                                slices, [&](uint64_t o0, uint64_t o1) { on_slice(ctx, o0, o1); });
+}
+
 uint64_t scratch_bytes_kv(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<KV64>(n, sort_n, fan);
 }

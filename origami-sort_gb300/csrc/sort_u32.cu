@@ -23,6 +23,13 @@ uint64_t scratch_bytes_io_u32(uint64_t n, uint64_t sort_n, int fan, uint64_t sta
 
 uint64_t tile_u32() { return k1_tile<uint32_t>(); }
 
+cudaError_t kway_final_u32(const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
+                          void* scratch, cudaStream_t st, int slices, void (*on_slice)(void*, uint64_t, uint64_t),
+                          void* ctx) {
+    return kway_pass_sliced<uint32_t>(static_cast<const uint32_t*>(in), static_cast<uint32_t*>(out), n, run, fan, xout, scratch, st,
+                                slices, [&](uint64_t o0, uint64_t o1) { on_slice(ctx, o0, o1); });
+}
+
 uint64_t scratch_bytes_u32(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint32_t>(n, sort_n, fan);
 }

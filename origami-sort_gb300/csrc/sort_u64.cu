@@ -23,6 +23,13 @@ uint64_t scratch_bytes_io_u64(uint64_t n, uint64_t sort_n, int fan, uint64_t sta
 
 uint64_t tile_u64() { return k1_tile<uint64_t>(); }
 
+cudaError_t kway_final_u64(const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
+                          void* scratch, cudaStream_t st, int slices, void (*on_slice)(void*, uint64_t, uint64_t),
+                          void* ctx) {
+    return kway_pass_sliced<uint64_t>(static_cast<const uint64_t*>(in), static_cast<uint64_t*>(out), n, run, fan, xout, scratch, st,
+                                slices, [&](uint64_t o0, uint64_t o1) { on_slice(ctx, o0, o1); });
+}
+
 uint64_t scratch_bytes_u64(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint64_t>(n, sort_n, fan);
 }
