@@ -7,20 +7,34 @@
 
 namespace origami {
 
+// Grids of the strided kernels: every SM full (resident CTAs per SM x SMs).
 template <class T>
-int seg_grid() {
-    static int g = 0;
-    if (g == 0) {
+struct SegGrids {
+    int tile = 0, merge = 0, part = 0;
+};
+
+template <class T>
+const SegGrids<T>& seg_grids() {
+    static SegGrids<T> g;
+    if (g.tile == 0) {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(seg_persistent_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)SegShape<T>::SMEM);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_persistent_kernel<T>, SegShape<T>::NT,
-                                                      SegShape<T>::SMEM);
-        g = sms * (per > 0 ? per : 1);
+        cudaFuncSetAttribute(seg_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SegShape<T>::SMEM);
+        cudaFuncSetAttribute(seg_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape<T>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_tile_kernel<T>, SegShape<T>::NT, SegShape<T>::SMEM);
+        const int tile = sms * (per > 0 ? per : 1);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T>, Config<T>::P_NT, PShape<T>::SMEM);
+        g.merge = sms * (per > 0 ? per : 1);
+        g.part = sms * 8;
+        g.tile = tile;
     }
     return g;
+}
+
+template <class T>
+int seg_grid() {
+    return seg_grids<T>().tile;
 }
 
 // Sorts every segment of d in place (result in d; tmp is the ping-pong
@@ -30,19 +44,25 @@ cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t 
                      void* scratch, int maxl, cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
     SegState s = seg_state<T>(scratch, off, n, nseg, maxl);
+    const SegGrids<T>& g = seg_grids<T>();
     cudaMemsetAsync(s.err, 0, sizeof(int), st);
     const unsigned b = (unsigned)((nseg + 255) / 256);
     static const std::string n_plan = std::string("seg_plan<") + TypeName<T>::v + ">";
     static const std::string n_scan = std::string("seg_scan<") + TypeName<T>::v + ">";
-    static const std::string n_fill = std::string("seg_fill<") + TypeName<T>::v + ">";
-    static const std::string n_run = std::string("seg_persistent<") + TypeName<T>::v + ">";
+    static const std::string n_tile = std::string("seg_tile<") + TypeName<T>::v + ">";
+    static const std::string n_part = std::string("seg_partition<") + TypeName<T>::v + ">";
+    static const std::string n_merge = std::string("seg_merge<") + TypeName<T>::v + ">";
     launch(n_plan.c_str(), st, [&] { seg_plan_kernel<T><<<b, 256, 0, st>>>(s); });
-    launch(n_scan.c_str(), st, [&] { seg_scan_kernel<T><<<(unsigned)(maxl + 2), 1024, 0, st>>>(s); });
-    launch(n_fill.c_str(), st, [&] { seg_fill_kernel<T><<<b, 256, 0, st>>>(s); });
-    const int grid = seg_grid<T>();
-    launch(n_run.c_str(), st, [&] {
-        seg_persistent_kernel<T><<<grid, SegShape<T>::NT, SegShape<T>::SMEM, st>>>(s, d, tmp, xmask);
+    launch(n_scan.c_str(), st, [&] { seg_scan_kernel<T><<<(unsigned)(maxl + 1), 1024, 0, st>>>(s); });
+    launch(n_tile.c_str(), st, [&] {
+        seg_tile_kernel<T><<<g.tile, SegShape<T>::NT, SegShape<T>::SMEM, st>>>(s, d, tmp, xmask);
     });
+    for (int l = 0; l < maxl; ++l) {
+        launch(n_part.c_str(), st, [&] { seg_part_kernel<T><<<g.part, 256, 0, st>>>(s, l, d, tmp); });
+        launch(n_merge.c_str(), st, [&] {
+            seg_merge_kernel<T><<<g.merge, Config<T>::P_NT, PShape<T>::SMEM, st>>>(s, l, d, tmp, xmask);
+        });
+    }
     return cudaGetLastError();
 }
 

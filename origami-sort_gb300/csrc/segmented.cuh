@@ -1,25 +1,29 @@
-// Batched segmented sort: many independent arrays of uneven length, sorted by
-// ONE persistent launch that pulls jobs from a device work queue.
+// Batched segmented sort: many independent arrays of uneven length, sorted
+// together, level by level, with the plain sort's tile bodies.
 //
-// Segment s is items [off[s], off[s+1]) of the caller's buffer. Size classes:
-//   warp    len <= 32*WVT      one warp sorts it in registers (warp_sort.cuh)
-//   tile    len <= TILE        one CTA sorts it (register + shared-memory tile sort)
-//   large   len >  TILE        ceil(len/TILE) tile jobs, then L = ceil(log2(tiles))
-//                              binary merge levels of ceil(len/MT) merge jobs each
-// Queue A holds CTA jobs in dependency order: every tile job first, then merge
-// level 0 of every large segment, level 1, ... A merge job of level l may start
-// once its segment has finished all tile jobs and levels < l (a per-segment
-// completion counter). Jobs are handed out in increasing order and never
-// depend on later ones, so every wait is for work already running on some
-// CTA; waits are still bounded (clock budget, then an error flag and exit).
-// Queue B holds the warp-class segments; warps take them once queue A is empty.
+// Segment s is items [off[s], off[s+1]) of the caller's buffer d. With T1 the
+// tile of the first kernel (8192 / 4096 / 2048 items) and MT the merge tile
+// of a binary pass (pipeline.cuh):
+//   tile phase   every segment is cut into ceil(len / T1) tiles (a short
+//                segment is one partial tile); one CTA sorts a tile in
+//                registers and shared memory;
+//   level l      every segment longer than T1 << l merges its runs of
+//                T1 << l pairwise: a partition kernel finds each output tile's
+//                merge-path split, a merge kernel merges the tiles (the
+//                binary-pass merge body: shared-memory staging, output written
+//                over the input, one block per thread).
+// A segment with L levels alternates between d and tmp so that its last step
+// writes d: its tiles go to tmp when L is odd.
 //
-// The job lists are built on the device (plan -> per-class scans -> fill), so
-// the whole batched call is a fixed sequence of launches and can be captured
-// in a CUDA graph.
+// Each kernel is launched once per phase or level for all segments together,
+// with a fixed grid that strides over that phase's job list. The job lists are
+// counted on the device (plan, then one prefix scan per list), so the host
+// never waits and the whole sequence can be captured in a CUDA graph. A level
+// that no segment needs finds an empty list and returns at once.
 #pragma once
 #include "common.cuh"
 #include "merge_core.cuh"
+#include "pipeline.cuh"
 #include "warp_sort.cuh"
 
 namespace origami {
@@ -30,75 +34,83 @@ template <>
 struct SegCfg<uint32_t> {
     static constexpr int NW = 8, VT = 32;  // tile: 8 warps x 32 lanes x 32 keys = 8192
     static constexpr int TILE = NW * 32 * VT;
-    static constexpr int MT = 8192;        // merge job output tile
-    static constexpr bool WARP_CLASS = true;
     static constexpr bool STABLE = false;
+    static constexpr int TILE_MINB = 3, MERGE_MINB = 8;  // CTAs per SM the register budget allows
 };
 template <>
 struct SegCfg<uint64_t> {
     static constexpr int NW = 8, VT = 16;  // 4096
     static constexpr int TILE = NW * 32 * VT;
-    static constexpr int MT = 4096;
-    static constexpr bool WARP_CLASS = true;
     static constexpr bool STABLE = false;
+    static constexpr int TILE_MINB = 2, MERGE_MINB = 8;
 };
 template <>
 struct SegCfg<KV64> {
-    static constexpr int NW = 8, VT = 8;   // 2048, stable block sort
+    static constexpr int NW = 8, VT = 8;  // 2048, stable block sort
     static constexpr int TILE = NW * 32 * VT;
-    static constexpr int MT = 2048;
-    static constexpr bool WARP_CLASS = false;
     static constexpr bool STABLE = true;
+    static constexpr int TILE_MINB = 3, MERGE_MINB = 6;
 };
 
+// Merge levels for a segment of len items (runs of TILE doubled until one).
 template <class T>
-inline int seg_levels_for(uint64_t len) {
+__host__ __device__ inline int seg_levels_for(uint64_t len) {
     const uint64_t tiles = (len + SegCfg<T>::TILE - 1) / SegCfg<T>::TILE;
     int l = 0;
     while ((1ull << l) < tiles) ++l;
     return l;
 }
 
-// Device-resident plan and queue state (all pointers into one scratch block).
+// Device-resident plan (all pointers into one scratch block).
 struct SegState {
-    const uint64_t* off;   // [nseg+1] segment offsets (caller's)
-    uint64_t n;            // items in the buffers: every segment must lie in [0, n)
+    const uint64_t* off;  // [nseg+1] segment offsets (caller's)
+    uint64_t n;           // items in the buffers: every segment must lie in [0, n)
     uint32_t nseg;
-    int maxl;              // merge levels planned for
-    uint32_t* cnt;         // [(maxl+2) * nseg] per-class job counts, then prefixes
-    uint32_t* tot;         // [maxl+2] class totals: 0 = tile jobs, 1 = warp segs, 2+l = level l
-    uint64_t* jobs;        // queue A: (segment << 32 | local index)
-    uint32_t* wsegs;       // queue B: warp-class segment ids
-    uint32_t* done;        // [nseg] finished CTA jobs per segment
-    uint32_t* heads;       // [2] queue heads
-    int* err;              // 1 = wait budget exhausted
+    int maxl;             // merge levels planned for
+    uint32_t* cnt;        // [(maxl+1) * nseg] jobs per segment: row 0 tiles, row 1+l
+                          // level-l merge tiles; exclusive prefixes after the scan
+    uint32_t* tot;        // [maxl+1] jobs per row
+    int64_t* splits;      // merge-path split of each merge tile of the current level
+    uint32_t* segof;      // segment of each merge tile of the current level
+    int* err;             // 2 = bad offsets
 };
 
 template <class T>
 struct SegGeom {
     uint64_t len;
-    uint32_t tiles, levels, mjobs;
-    int cls;  // 0 warp, 1 tile, 2 large
+    uint32_t tiles, levels, mtiles;
     // An invalid segment (decreasing offsets or past the buffer) is treated as
     // empty; the plan kernel reports it.
     __device__ __forceinline__ SegGeom(const uint64_t* off, uint32_t s, uint64_t n) {
-        using C = SegCfg<T>;
         const uint64_t a = off[s], b = off[s + 1];
         len = (a <= b && b <= n) ? b - a : 0;
-        tiles = (uint32_t)((len + C::TILE - 1) / C::TILE);
-        levels = 0;
-        while ((1ull << levels) < tiles) ++levels;
-        mjobs = (uint32_t)((len + C::MT - 1) / C::MT);
-        if (C::WARP_CLASS && len <= 32ull * C::VT)
-            cls = 0;
-        else if (len <= (uint64_t)C::TILE)
-            cls = 1;
-        else
-            cls = 2;
+        tiles = (uint32_t)((len + SegCfg<T>::TILE - 1) / SegCfg<T>::TILE);
+        levels = (uint32_t)seg_levels_for<T>(len);
+        mtiles = (uint32_t)((len + Config<T>::P_TILE - 1) / Config<T>::P_TILE);
     }
 };
 
-// 1. per segment: job counts of every class (cnt[q * nseg + s])
+// The segment whose job range [pref[s], pref[s] + cnt[s]) holds job j
+// (segments without jobs have empty ranges and are skipped).
+__device__ __forceinline__ uint32_t seg_of_job(const uint32_t* pref, uint32_t nseg, uint32_t j) {
+    uint32_t a = 0, e = nseg;
+    while (a < e) {
+        const uint32_t m = (a + e) >> 1;
+        if (pref[m] <= j)
+            a = m + 1;
+        else
+            e = m;
+    }
+    return a - 1;
+}
+
+// Buffer a segment with L levels holds after step k (0 = tile phase).
+template <class T>
+__device__ __forceinline__ T* seg_buf(uint32_t L, uint32_t k, T* d, T* tmp) {
+    return ((L - k) & 1) ? tmp : d;
+}
+
+// 1. per segment: jobs of every row
 template <class T>
 __global__ void seg_plan_kernel(SegState st) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -106,14 +118,12 @@ __global__ void seg_plan_kernel(SegState st) {
     if (st.off[s + 1] < st.off[s] || st.off[s + 1] > st.n) atomicExch(st.err, 2);
     const SegGeom<T> g(st.off, s, st.n);
     const uint32_t n = st.nseg;
-    st.cnt[0 * n + s] = (g.cls == 0) ? 0u : (g.cls == 1 ? 1u : g.tiles);
-    st.cnt[1 * n + s] = (g.cls == 0) ? 1u : 0u;
-    for (int l = 0; l < st.maxl; ++l) st.cnt[(2 + l) * n + s] = (g.cls == 2 && (uint32_t)l < g.levels) ? g.mjobs : 0u;
-    st.done[s] = 0;
+    st.cnt[s] = g.tiles;
+    for (int l = 0; l < st.maxl; ++l) st.cnt[(1 + l) * (size_t)n + s] = ((uint32_t)l < g.levels) ? g.mtiles : 0u;
 }
 
-// 2. exclusive scan of one class per block (block q scans cnt[q*nseg ..]); the
-//    class total goes to tot[q]. 1024 threads, chunked.
+// 2. exclusive scan of one row per block (block q scans row q); the row total
+//    goes to tot[q]. 1024 threads, chunked.
 template <class T>
 __global__ void __launch_bounds__(1024) seg_scan_kernel(SegState st) {
     __shared__ uint32_t part[1024];
@@ -138,64 +148,18 @@ __global__ void __launch_bounds__(1024) seg_scan_kernel(SegState st) {
         acc += v;
     }
     if (threadIdx.x == 1023) st.tot[blockIdx.x] = part[1023];
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        st.heads[0] = 0;
-        st.heads[1] = 0;
-    }
 }
 
-// 3. fill the queues: queue A = [tile jobs | level 0 | level 1 | ...]
-template <class T>
-__global__ void seg_fill_kernel(SegState st) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= st.nseg) return;
-    const SegGeom<T> g(st.off, s, st.n);
-    const uint32_t n = st.nseg;
-    if (g.cls == 0) {
-        st.wsegs[st.cnt[1 * n + s]] = s;
-        return;
-    }
-    uint64_t base = st.cnt[0 * n + s];
-    const uint32_t nt = (g.cls == 1) ? 1u : g.tiles;
-    for (uint32_t t = 0; t < nt; ++t) st.jobs[base + t] = ((uint64_t)s << 32) | t;
-    uint64_t lvl_base = st.tot[0];
-    for (int l = 0; l < st.maxl; ++l) {
-        if (g.cls == 2 && (uint32_t)l < g.levels) {
-            const uint64_t b = lvl_base + st.cnt[(2 + l) * n + s];
-            for (uint32_t t = 0; t < g.mjobs; ++t) st.jobs[b + t] = ((uint64_t)s << 32) | t;
-        }
-        lvl_base += st.tot[2 + l];
-    }
-}
-
-// ------------------------------------------------------ persistent kernel --
+// ------------------------------------------------------------ tile phase --
 template <class T>
 struct SegShape {
     using C = SegCfg<T>;
     static constexpr int NT = C::NW * 32;
     static constexpr int BUF = padded_items<T>(C::TILE + C::VT + 1);
     static constexpr size_t BUF_BYTES = (((size_t)BUF * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr int V = Vec<T>::N;
-    static constexpr int IN_CAP = C::MT + 4 * V + C::VT + 4;
-    static constexpr size_t IN_BYTES = (((size_t)IN_CAP * sizeof(T)) + 15) & ~(size_t)15;
-    static constexpr size_t SMEM = (2 * BUF_BYTES > IN_BYTES + BUF_BYTES) ? 2 * BUF_BYTES : IN_BYTES + BUF_BYTES;
+    static constexpr size_t SMEM = 2 * BUF_BYTES;
     static constexpr int SPLITS = C::TILE / (C::VT - 1) + C::TILE / (2 * C::VT) + 8;
 };
-
-// bounded wait on a completion counter (thread 0 only)
-__device__ __forceinline__ bool seg_wait(const uint32_t* ctr, uint32_t target, int* err) {
-    const long long budget = 2000000000ll;  // ~1 s of SM clock
-    const long long t0 = clock64();
-    while (*(volatile const uint32_t*)ctr < target) {
-        if (clock64() - t0 > budget || *(volatile int*)err) {
-            atomicExch(err, 1);
-            return false;
-        }
-        __nanosleep(200);
-    }
-    __threadfence();
-    return true;
-}
 
 // Sorts items [p0, p0+cnt) of `src` (cnt <= TILE) into `dst` at the same
 // positions: register/warp sort, then shared-memory rounds up to the tile.
@@ -263,174 +227,119 @@ __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
     }
 }
 
-// One warp sorts a whole segment of len <= 32*VT keys in registers.
-template <class T, int VT>
-__device__ __forceinline__ void seg_warp_sort(T* d, uint64_t base, int len, uint64_t xmask) {
-    const int lane = threadIdx.x & 31;
-    T v[VT];
-#pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const int i = lane * VT + k;
-        v[k] = (i < len) ? Traits<T>::flip(d[base + i], xmask) : Traits<T>::max_item();
-    }
-    warp_sort<T, VT>(v, 32 * VT);
-#pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const int i = lane * VT + k;
-        if (i < len) d[base + i] = Traits<T>::flip(v[k], xmask);
-    }
-}
-
+// 3. tile phase: a grid of CTAs strides over the tile jobs
 template <class T>
-__global__ void __launch_bounds__(SegShape<T>::NT) seg_persistent_kernel(SegState st, T* d, T* tmp,
-                                                                        uint64_t xmask) {
+__global__ void __launch_bounds__(SegShape<T>::NT, SegCfg<T>::TILE_MINB) seg_tile_kernel(SegState st, T* d, T* tmp,
+                                                                                         uint64_t xmask) {
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
-    constexpr int NT = Sh::NT, V = Sh::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int split[Sh::SPLITS];
-    __shared__ uint64_t job_s;
-    __shared__ int ok_s;
-    __shared__ int64_t msplit[2];
-    const int tid = threadIdx.x;
-    const uint32_t nA = st.tot[0] + [&] {
-        uint32_t t = 0;
-        for (int l = 0; l < st.maxl; ++l) t += st.tot[2 + l];
-        return t;
-    }();
-
-    // ---------------- queue A: CTA jobs
-    for (;;) {
-        if (tid == 0) {
-            const uint32_t j = atomicAdd(&st.heads[0], 1u);
-            job_s = (j < nA && !*(volatile int*)st.err) ? ((uint64_t)j | (1ull << 63)) : 0ull;
-        }
-        __syncthreads();
-        const uint64_t jw = job_s;
-        __syncthreads();
-        if (!(jw >> 63)) break;
-        const uint32_t j = (uint32_t)jw;
-        const uint64_t e = st.jobs[j];
-        const uint32_t s = (uint32_t)(e >> 32), t = (uint32_t)e;
+    const uint32_t total = st.tot[0];
+    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+        const uint32_t s = seg_of_job(st.cnt, st.nseg, j);
         const SegGeom<T> g(st.off, s, st.n);
-        const uint64_t base = st.off[s];
-        // buffer holding level l's input: tiles write to `first`, so the last
-        // level (or the tile sort itself) lands in d
-        T* first = (g.levels % 2 == 0) ? d : tmp;
-        if (j < st.tot[0]) {
-            // tile job: sort tile t of segment s (or the whole segment)
-            const uint64_t p0 = base + (uint64_t)t * C::TILE;
-            const int cnt = (int)min((uint64_t)C::TILE, g.len - (uint64_t)t * C::TILE);
-            const bool last = (g.levels == 0);
-            seg_tile_sort<T>(d, first, p0, cnt, xmask, last ? xmask : 0, smem_raw, split);
-        } else {
-            // merge job: level l, output tile t
-            int l = 0;
-            uint32_t acc = st.tot[0];
-            while (l + 1 < st.maxl && j >= acc + st.tot[2 + l]) acc += st.tot[2 + l++];
-            if (tid == 0) ok_s = seg_wait(&st.done[s], g.tiles + (uint32_t)l * g.mjobs, st.err);
-            __syncthreads();
-            if (!ok_s) break;
-            const T* src = ((l & 1) == 0) ? first : (first == d ? tmp : d);
-            T* dst = (src == d) ? tmp : d;
-            const uint64_t run = (uint64_t)C::TILE << l;
-            const uint64_t o = (uint64_t)t * C::MT;
-            const uint64_t pb = (o / (2 * run)) * (2 * run);
-            const uint64_t la = min(run, g.len - pb);
-            const uint64_t lb = min(run, g.len - pb - la);
-            const uint64_t d0 = o - pb;
-            const uint64_t d1 = min(d0 + (uint64_t)C::MT, la + lb);
-            const T* A = src + base + pb;
-            const T* B = A + la;
-            const int wid = tid >> 5;
-            if (wid < 2) {
-                const int64_t r = warp_merge_path(A, (int64_t)la, B, (int64_t)lb, (int64_t)(wid ? d1 : d0));
-                if ((tid & 31) == 0) msplit[wid] = r;
-            }
-            __syncthreads();
-            const int64_t a0 = msplit[0], a1 = msplit[1];
-            const int na = (int)(a1 - a0);
-            const int total = (int)(d1 - d0);
-            const int nb = total - na;
-            T* sin = reinterpret_cast<T*>(smem_raw);
-            T* sout = reinterpret_cast<T*>(smem_raw + Sh::IN_BYTES);
-            const int a_lead = stage_vec<T, NT>(sin, src, base + pb + (uint64_t)a0, na);
-            const int b_base = ((a_lead + na + V - 1) / V) * V;
-            const int b_lead = stage_vec<T, NT>(sin + b_base, src, base + pb + la + (d0 - (uint64_t)a0), nb);
-            cp_async_commit_all();
-            cp_async_wait_all();
-            __syncthreads();
-            merge_pair_round<T, NT, C::STABLE ? C::VT - 1 : C::VT, C::STABLE>(sin, a_lead, na, b_base + b_lead,
-                                                                               nb, sout, split);
-            const uint64_t xo = ((uint32_t)l + 1 == g.levels) ? xmask : 0;
-            T* op = dst + base + o;
-            for (int i = tid; i < total; i += NT) op[i] = Traits<T>::flip(sout[i], xo);
-        }
+        const uint32_t t = j - st.cnt[s];
+        const uint64_t p0 = st.off[s] + (uint64_t)t * C::TILE;
+        const int cnt = (int)min((uint64_t)C::TILE, g.len - (uint64_t)t * C::TILE);
+        seg_tile_sort<T>(d, seg_buf<T>(g.levels, 0, d, tmp), p0, cnt, xmask, g.levels == 0 ? xmask : 0, smem_raw,
+                         split);
         __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(&st.done[s], 1u);
-        }
-    }
-
-    // ---------------- queue B: warp-class segments, one warp each
-    if constexpr (C::WARP_CLASS) {
-        const int lane = tid & 31;
-        const uint32_t nB = st.tot[1];
-        for (;;) {
-            uint32_t j = 0;
-            if (lane == 0) j = atomicAdd(&st.heads[1], 1u);
-            j = __shfl_sync(0xFFFFFFFFu, j, 0);
-            if (j >= nB) break;
-            const uint32_t s = st.wsegs[j];
-            const uint64_t base = st.off[s];
-            const int len = (int)SegGeom<T>(st.off, s, st.n).len;
-            // smallest lane width that holds the segment
-            if (len <= 32 * 1)
-                seg_warp_sort<T, 1>(d, base, len, xmask);
-            else if (len <= 32 * 2)
-                seg_warp_sort<T, 2>(d, base, len, xmask);
-            else if (len <= 32 * 4)
-                seg_warp_sort<T, 4>(d, base, len, xmask);
-            else if (len <= 32 * 8)
-                seg_warp_sort<T, 8>(d, base, len, xmask);
-            else if (len <= 32 * 16)
-                seg_warp_sort<T, 16>(d, base, len, xmask);
-            else if constexpr (C::VT >= 32)
-                seg_warp_sort<T, 32>(d, base, len, xmask);
-        }
     }
 }
 
-}  // namespace origami
+// Geometry of merge tile u (MT outputs) of a segment of len items at level l.
+struct SegPair {
+    uint64_t pb, la, lb, d0, d1;
+    __device__ __forceinline__ SegPair(uint64_t len, uint64_t run, uint64_t u, uint64_t mt) {
+        const uint64_t o = u * mt;
+        pb = (o / (2 * run)) * (2 * run);
+        la = min(run, len - pb);
+        lb = min(run, len - pb - la);
+        d0 = o - pb;
+        d1 = min(d0 + mt, la + lb);
+    }
+};
 
-namespace origami {
-
-// Upper bound of queue A's length for nseg segments of n items in total.
+// 4. level l, partition: one thread per merge tile
 template <class T>
-inline uint64_t seg_max_jobs(uint64_t n, uint64_t nseg, int maxl) {
-    using C = SegCfg<T>;
-    return (n / C::TILE + nseg) + (uint64_t)maxl * (n / C::MT + nseg) + 16;
+__global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
+    const uint32_t* pref = st.cnt + (size_t)(1 + l) * st.nseg;
+    const uint32_t total = st.tot[1 + l];
+    const uint64_t run = (uint64_t)SegCfg<T>::TILE << l;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < total;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = seg_of_job(pref, st.nseg, (uint32_t)j);
+        const SegGeom<T> g(st.off, s, st.n);
+        const SegPair p(g.len, run, j - pref[s], Config<T>::P_TILE);
+        const T* A = seg_buf<const T>(g.levels, l, d, tmp) + st.off[s] + p.pb;
+        st.splits[j] = global_merge_path(A, (int64_t)p.la, A + p.la, (int64_t)p.lb, (int64_t)p.d0);
+        st.segof[j] = s;
+    }
 }
 
-// Scratch bytes for the plan and queues.
+// 5. level l, merge: a grid of CTAs strides over the merge tiles
+template <class T>
+__global__ void __launch_bounds__(Config<T>::P_NT, SegCfg<T>::MERGE_MINB) seg_merge_kernel(SegState st, int l, T* d,
+                                                                                           T* tmp, uint64_t xmask) {
+    using C = Config<T>;
+    using Sh = PShape<T>;
+    constexpr int NT = C::P_NT, V = Sh::V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int split[Sh::SPLITS];
+    T* sin = reinterpret_cast<T*>(smem_raw);
+    const int tid = threadIdx.x;
+    const uint32_t* pref = st.cnt + (size_t)(1 + l) * st.nseg;
+    const uint32_t total = st.tot[1 + l];
+    const uint64_t run = (uint64_t)SegCfg<T>::TILE << l;
+    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+        const uint32_t s = st.segof[j];
+        const SegGeom<T> g(st.off, s, st.n);
+        const SegPair p(g.len, run, j - pref[s], C::P_TILE);
+        const T* src = seg_buf<T>(g.levels, l, d, tmp);
+        T* dst = seg_buf<T>(g.levels, l + 1, d, tmp);
+        const uint64_t base = st.off[s] + p.pb;
+        const int64_t a0 = st.splits[j];
+        const int64_t a1 = (p.d1 < p.la + p.lb) ? st.splits[j + 1] : (int64_t)p.la;  // next tile, same pair
+        const int na = (int)(a1 - a0);
+        const int tot = (int)(p.d1 - p.d0);
+        const int nb = tot - na;
+        const int a_lead = stage_vec<T, NT>(sin, src, base + (uint64_t)a0, na);
+        const int b_base = ((a_lead + na + V - 1) / V) * V;
+        const int b_lead = stage_vec<T, NT>(sin + b_base, src, base + p.la + (p.d0 - (uint64_t)a0), nb);
+        cp_async_commit_all();
+        cp_async_wait_all();
+        __syncthreads();
+        merge_pair_round_inplace<T, NT, C::P_VT, C::STABLE>(sin, a_lead, na, b_base + b_lead, nb, split);
+        const uint64_t xo = ((uint32_t)l + 1 == g.levels) ? xmask : 0;
+        T* op = dst + base + p.d0;  // any alignment: plain coalesced stores
+        for (int i = tid; i < tot; i += NT) op[i] = Traits<T>::flip(sin[i], xo);
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ scratch ----
+template <class T>
+inline uint64_t seg_tile_slots(uint64_t n, uint64_t nseg) {
+    return n / Config<T>::P_TILE + nseg + 2;  // merge tiles of one level, upper bound
+}
+
 template <class T>
 inline uint64_t seg_scratch_bytes(uint64_t n, uint64_t nseg, int maxl) {
-    const uint64_t q = (uint64_t)maxl + 2;
+    const uint64_t q = (uint64_t)maxl + 1;
     uint64_t b = 0;
-    b += ((q * nseg * 4 + 255) & ~255ull);              // cnt
-    b += ((q * 4 + 255) & ~255ull);                     // tot
-    b += ((seg_max_jobs<T>(n, nseg, maxl) * 8 + 255) & ~255ull);  // jobs
-    b += ((nseg * 4 + 255) & ~255ull);                  // wsegs
-    b += ((nseg * 4 + 255) & ~255ull);                  // done
-    b += 256;                                           // heads, err
+    b += ((q * nseg * 4 + 255) & ~255ull);                      // cnt
+    b += ((q * 4 + 255) & ~255ull);                             // tot
+    b += ((seg_tile_slots<T>(n, nseg) * 8 + 255) & ~255ull);    // splits
+    b += ((seg_tile_slots<T>(n, nseg) * 4 + 255) & ~255ull);    // segof
+    b += 256;                                                   // err
     return b;
 }
 
 template <class T>
 inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64_t nseg, int maxl) {
     SegState s;
-    const uint64_t q = (uint64_t)maxl + 2;
+    const uint64_t q = (uint64_t)maxl + 1;
     char* p = static_cast<char*>(scratch);
     auto take = [&](uint64_t bytes) {
         char* r = p;
@@ -443,12 +352,9 @@ inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64
     s.maxl = maxl;
     s.cnt = reinterpret_cast<uint32_t*>(take(q * nseg * 4));
     s.tot = reinterpret_cast<uint32_t*>(take(q * 4));
-    s.jobs = reinterpret_cast<uint64_t*>(take(seg_max_jobs<T>(n, nseg, maxl) * 8));
-    s.wsegs = reinterpret_cast<uint32_t*>(take(nseg * 4));
-    s.done = reinterpret_cast<uint32_t*>(take(nseg * 4));
-    char* tail = take(256);
-    s.heads = reinterpret_cast<uint32_t*>(tail);
-    s.err = reinterpret_cast<int*>(tail + 16);
+    s.splits = reinterpret_cast<int64_t*>(take(seg_tile_slots<T>(n, nseg) * 8));
+    s.segof = reinterpret_cast<uint32_t*>(take(seg_tile_slots<T>(n, nseg) * 4));
+    s.err = reinterpret_cast<int*>(take(256));
     return s;
 }
 

@@ -34,7 +34,7 @@ uint64_t scratch_bytes_kv(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<KV64>(n, sort_n, fan);
 }
 
-int seg_levels_kv(uint64_t n) { return seg_levels_for<KV64>(n) + 1; }
+int seg_levels_kv(uint64_t n) { return seg_levels_for<KV64>(n); }
 
 uint64_t seg_scratch_bytes_kv(uint64_t n, uint64_t nseg, int maxl) {
     return seg_scratch_bytes<KV64>(n, nseg, maxl);

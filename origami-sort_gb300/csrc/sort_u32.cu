@@ -34,7 +34,7 @@ uint64_t scratch_bytes_u32(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint32_t>(n, sort_n, fan);
 }
 
-int seg_levels_u32(uint64_t n) { return seg_levels_for<uint32_t>(n) + 1; }
+int seg_levels_u32(uint64_t n) { return seg_levels_for<uint32_t>(n); }
 
 uint64_t seg_scratch_bytes_u32(uint64_t n, uint64_t nseg, int maxl) {
     return seg_scratch_bytes<uint32_t>(n, nseg, maxl);
