@@ -283,6 +283,28 @@ int origami_server_destroy(origami_server* s);
  */
 int origami_generate_device(int kind, void* d, uint64_t n, int dist, uint64_t seed, void* stream);
 
+/*
+ * Autotuning (no counterpart in the reference, whose tuning is compile-time
+ * config.h constants and the bench_sort_phases switch-point sweeps). Every
+ * sort with min_k = 0 takes its pass shape from a table indexed by item kind
+ * and size class floor(log2 n): the merge fan-in (2 = binary passes, 4/8/16 =
+ * k-way passes) and, for binary passes, one of two tile shapes (threads,
+ * items per thread, tile; 0 is the default). min_k = 2 keeps the table's tile
+ * shape with binary passes; larger min_k forces that fan-in.
+ *   origami_autotune   times every shape on n generated device items and stores
+ *                      the fastest for n's size class; `report` (may be NULL)
+ *                      receives one "fan= variant= ms=" line per shape.
+ *   get / set          read or write one entry.
+ *   save / load        the non-default entries as "kind class fan variant"
+ *                      lines. The file named by ORIGAMI_TUNING, if set, is
+ *                      loaded at first use.
+ */
+int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap);
+int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant);
+int origami_tuning_set(int kind, uint64_t n, int fan, int variant);
+int origami_tuning_save(const char* path);
+int origami_tuning_load(const char* path);
+
 /* Device arena used by the host-pointer calls and by the serving loop. */
 int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */
 int origami_arena_trim(void);               /* return cached memory to the driver */

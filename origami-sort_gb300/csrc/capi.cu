@@ -1,5 +1,6 @@
 // C ABI (include/origami_gpu.h): argument validation, the pooled device arena,
 // host-pointer staging and dispatch onto the typed pipelines.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -114,6 +115,15 @@ unsigned item_bytes(int kind) {
     }
 }
 
+uint64_t k1_tile_of(int kind) {
+    switch (kind) {
+        case ORIGAMI_U32: return tile_u32();
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return tile_u64();
+        default: return tile_kv();
+    }
+}
+
 uint64_t key_mask(int kind) {
     return (kind == ORIGAMI_I64 || kind == ORIGAMI_KV64) ? 0x8000000000000000ull : 0ull;
 }
@@ -181,13 +191,37 @@ int check_args(int kind, const void* d, const void* tmp, uint64_t n, uint64_t so
 }
 
 // Merge fan-in for a min_k request: 2 keeps binary passes, 3..16 round up to
-// a power of two, larger values are capped at 16; 0 selects the default.
+// a power of two, larger values are capped at 16.
 int fan_of(unsigned min_k) {
-    if (min_k == 0) return 2;  // tuned default: binary passes are the fastest path today
     if (min_k <= 2) return 2;
     int f = 4;
     while ((unsigned)f < min_k && f < 16) f <<= 1;
     return f;
+}
+
+// ---- tuning table: pass shape per kind and size class (floor(log2 n)) ----
+// Default: binary passes with the first tile shape (the measured best at
+// 1 GiB). origami_autotune() times the candidates and stores the winner.
+constexpr int TUNE_CLASSES = 41;
+std::atomic<int> g_tune[5][TUNE_CLASSES];
+std::once_flag g_tune_once;
+
+int size_class(uint64_t n) {
+    int c = 0;
+    while (c + 1 < TUNE_CLASSES && (2ull << c) <= n) ++c;
+    return c;
+}
+
+void tune_init();
+
+// Pass shape code for a sort of n items: min_k = 0 takes the table's choice,
+// min_k <= 2 binary passes with the table's tile shape, larger min_k k-way.
+int shape_for(int kind, uint64_t n, unsigned min_k) {
+    std::call_once(g_tune_once, tune_init);
+    const int code = g_tune[kind][size_class(n)].load(std::memory_order_relaxed);
+    if (min_k == 0) return code;
+    if (min_k <= 2) return shape_code(2, shape_fan(code) == 2 ? shape_variant(code) : 0);
+    return shape_code(fan_of(min_k), 0);
 }
 
 cudaError_t run_typed(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, void* want,
@@ -244,7 +278,7 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
     }
     void* scratch = nullptr;
     if (!tmp) CK(cudaMallocAsync(&scratch, n * item_bytes(kind), st), "scratch allocation");
-    const int fan = fan_of(min_k);
+    const int fan = shape_for(kind, n, min_k);
     void* work = nullptr;
     cudaError_t e = cudaMallocAsync(&work, scratch_bytes(kind, n, sort_n, fan), st);
     if (e != cudaSuccess) {
@@ -366,12 +400,12 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                      uint64_t sort_n, unsigned min_k, cudaStream_t st) {
     const uint64_t ib = item_bytes(kind);
     const uint64_t bytes = n * ib;
-    const int fan = fan_of(min_k);
+    const int fan = shape_for(kind, n, min_k);
     const uint64_t m = key_mask(kind);
     const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
     uint64_t chunk_n = 1ull << 22;
     while (chunk_n * 16 <= n) chunk_n <<= 1;  // 8 to 16 chunks
-    const bool chunked = fan == 2 && n >= 4 * chunk_n && limit > chunk_n;
+    const bool chunked = shape_fan(fan) == 2 && n >= 4 * chunk_n && limit > chunk_n;
     void *A = nullptr, *B = nullptr, *w0 = nullptr, *w1 = nullptr, *wm = nullptr;
     CK(cudaMallocAsync(&A, bytes, st), "arena allocation");
     cudaError_t e = cudaMallocAsync(&B, bytes, st);
@@ -379,7 +413,8 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
         if (e == cudaSuccess) e = cudaMallocAsync(&w0, typed_scratch_io(kind, n, sort_n, fan, 0), st);
         if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w0, st);
     } else {
-        const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, fan, 0);
+        const int cfan = shape_for(kind, chunk_n, min_k);  // the chunks' own tuned shape
+        const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, cfan, 0);
         if (e == cudaSuccess) e = cudaMallocAsync(&w0, cs, st);
         if (e == cudaSuccess) e = cudaMallocAsync(&w1, cs, st);
         // the merges across chunks are one k-way pass: bound by the host link
@@ -416,7 +451,7 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                 src = a + off * ib;
             }
             if (e == cudaSuccess)
-                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, fan,
+                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, cfan,
                              (c & 1) ? w1 : w0, cst);
         }
         if (e == cudaSuccess) {
@@ -451,6 +486,28 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
     if (e != cudaSuccess) return cuda_fail(e, "host sort");
     if (es != cudaSuccess) return cuda_fail(es, "stream sync");
     return ORIGAMI_OK;
+}
+
+// Table entries of a tuning file: one "kind size_class fan variant" line each.
+int tune_load_file(const char* path) {
+    FILE* f = std::fopen(path, "r");
+    if (!f) return fail(ORIGAMI_ERR_INVALID, "cannot open tuning file %s", path);
+    int kind, cls, fan, var, loaded = 0;
+    while (std::fscanf(f, "%d %d %d %d", &kind, &cls, &fan, &var) == 4) {
+        if (kind < 0 || kind > 4 || cls < 0 || cls >= TUNE_CLASSES) continue;
+        if (fan != 2 && fan != 4 && fan != 8 && fan != 16) continue;
+        if (var < 0 || var > 1 || (fan != 2 && var != 0)) continue;
+        g_tune[kind][cls].store(shape_code(fan, var), std::memory_order_relaxed);
+        ++loaded;
+    }
+    std::fclose(f);
+    return loaded;
+}
+
+void tune_init() {
+    for (auto& row : g_tune)
+        for (auto& c : row) c.store(shape_code(2, 0), std::memory_order_relaxed);
+    if (const char* path = std::getenv("ORIGAMI_TUNING")) tune_load_file(path);
 }
 
 // Host buffers: stage through the arena, sort on the device, copy the result
@@ -749,5 +806,114 @@ int origami_profile_report(char* buf, uint64_t cap) {
 }
 
 uint64_t origami_launch_count(void) { return g_launches.load(); }
+
+// ------------------------------------------------------------- tuning --
+int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    const int code = shape_for(kind, n, 0);
+    if (fan) *fan = shape_fan(code);
+    if (variant) *variant = shape_variant(code);
+    return ORIGAMI_OK;
+}
+
+int origami_tuning_set(int kind, uint64_t n, int fan, int variant) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (fan != 2 && fan != 4 && fan != 8 && fan != 16) return fail(ORIGAMI_ERR_INVALID, "fan must be 2, 4, 8 or 16");
+    if (variant < 0 || variant > 1 || (fan != 2 && variant != 0))
+        return fail(ORIGAMI_ERR_INVALID, "variant must be 0 or 1 (1 only with fan 2)");
+    std::call_once(g_tune_once, tune_init);
+    g_tune[kind][size_class(n)].store(shape_code(fan, variant), std::memory_order_relaxed);
+    return ORIGAMI_OK;
+}
+
+int origami_tuning_save(const char* path) {
+    if (!path) return fail(ORIGAMI_ERR_INVALID, "path is NULL");
+    std::call_once(g_tune_once, tune_init);
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(ORIGAMI_ERR_INVALID, "cannot write tuning file %s", path);
+    for (int k = 0; k < 5; ++k)
+        for (int c = 0; c < TUNE_CLASSES; ++c) {
+            const int code = g_tune[k][c].load(std::memory_order_relaxed);
+            if (code != shape_code(2, 0)) std::fprintf(f, "%d %d %d %d\n", k, c, shape_fan(code), shape_variant(code));
+        }
+    std::fclose(f);
+    return ORIGAMI_OK;
+}
+
+int origami_tuning_load(const char* path) {
+    if (!path) return fail(ORIGAMI_ERR_INVALID, "path is NULL");
+    std::call_once(g_tune_once, tune_init);
+    const int r = tune_load_file(path);
+    return r < 0 ? r : ORIGAMI_OK;
+}
+
+// Times every pass shape on n uniform device items of `kind` (binary passes
+// with either tile shape, k-way passes with fan-in 4, 8, 16; each the best of
+// three sorts after a warm-up) and stores the fastest for n's size class.
+int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (n < 2) return fail(ORIGAMI_ERR_INVALID, "autotune needs at least 2 items");
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    std::call_once(g_tune_once, tune_init);
+    const uint64_t bytes = n * item_bytes(kind);
+    cudaStream_t st = worker_stream();
+    void *p = nullptr, *d = nullptr, *t = nullptr, *work = nullptr;
+    CK(cudaMallocAsync(&p, bytes, st), "autotune buffers");
+    cudaError_t e = cudaMallocAsync(&d, bytes, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&t, bytes, st);
+    const int codes[] = {shape_code(2, 0), shape_code(2, 1), shape_code(4, 0), shape_code(8, 0), shape_code(16, 0)};
+    uint64_t wbytes = 0;
+    for (int c : codes) wbytes = std::max<uint64_t>(wbytes, scratch_bytes(kind, n, 0, c));
+    if (e == cudaSuccess) e = cudaMallocAsync(&work, wbytes, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && origami_generate_device(kind, p, n, 1, 2024, st) != ORIGAMI_OK) e = cudaErrorUnknown;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    std::string rep;
+    int best = codes[0];
+    float best_ms = 1e30f;
+    for (int c : codes) {
+        if (e != cudaSuccess) break;
+        if (shape_fan(c) > 2 && (n + k1_tile_of(kind) - 1) / k1_tile_of(kind) <= 2) continue;  // one level
+        float ms_best = 1e30f;
+        for (int it = 0; it < 4 && e == cudaSuccess; ++it) {
+            e = cudaMemcpyAsync(d, p, bytes, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaEventRecord(a, st);
+            if (e == cudaSuccess) e = run_typed(kind, d, t, n, 0, d, c, work, st);
+            if (e == cudaSuccess) e = cudaEventRecord(b, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0;
+            if (e == cudaSuccess && it > 0 && cudaEventElapsedTime(&ms, a, b) == cudaSuccess) ms_best = std::min(ms_best, ms);
+        }
+        char line[128];
+        std::snprintf(line, sizeof line, "fan=%d variant=%d ms=%.4f\n", shape_fan(c), shape_variant(c), ms_best);
+        rep += line;
+        if (ms_best < best_ms) {
+            best_ms = ms_best;
+            best = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (work) cudaFreeAsync(work, st);
+    if (t) cudaFreeAsync(t, st);
+    if (d) cudaFreeAsync(d, st);
+    cudaFreeAsync(p, st);
+    const cudaError_t es = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    if (es != cudaSuccess) return cuda_fail(es, "autotune");
+    g_tune[kind][size_class(n)].store(best, std::memory_order_relaxed);
+    char line[128];
+    std::snprintf(line, sizeof line, "chosen fan=%d variant=%d size_class=%d\n", shape_fan(best), shape_variant(best),
+                  size_class(n));
+    rep += line;
+    if (report && cap) {
+        std::strncpy(report, rep.c_str(), cap - 1);
+        report[cap - 1] = 0;
+    }
+    return ORIGAMI_OK;
+}
 
 }  // extern "C"

@@ -28,6 +28,7 @@ struct Config<uint32_t> {
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 32, K1_MINB = 3;
     static constexpr int K1_NT = 256, K1_VTS = 32, K1_VTM = 32;  // (block K1, unused)
     static constexpr int P_NT = 160, P_VT = 32, P_TILE = 4096, P_MINB = 1;  // binary pass tiles
+    static constexpr int P2_NT = 288, P2_VT = 32, P2_TILE = 8192, P2_MINB = 5;  // second tile shape
     static constexpr bool STABLE = false;
 };
 template <>
@@ -36,6 +37,7 @@ struct Config<uint64_t> {
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 1;
     static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
     static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 8;
+    static constexpr int P2_NT = 160, P2_VT = 32, P2_TILE = 4096, P2_MINB = 1;
     static constexpr bool STABLE = false;
 };
 template <>
@@ -44,6 +46,7 @@ struct Config<KV64> {
     static constexpr int K1_NW = 8, K1_NWT = 8, K1_VT = 8, K1_MINB = 1;
     static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 7;  // 2048 items (32 KiB)
     static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 1;  // serial merge blocks of 11
+    static constexpr int P2_NT = 160, P2_VT = 7, P2_TILE = 1024, P2_MINB = 8;
     static constexpr bool STABLE = true;
 };
 
@@ -69,6 +72,18 @@ template <class T>
 constexpr size_t merge_smem() {
     return PShape<T>::SMEM;
 }
+template <class T>
+using PShape2 = PairShape<T, Config<T>::P2_NT, Config<T>::P2_VT, Config<T>::STABLE, Config<T>::P2_TILE>;
+static_assert(Config<uint32_t>::P2_TILE >= Config<uint32_t>::P_TILE && Config<uint64_t>::P2_TILE >= Config<uint64_t>::P_TILE &&
+                  Config<KV64>::P2_TILE >= Config<KV64>::P_TILE,
+              "the splitter array is sized by the first (smallest) tile");
+
+// A pass shape code: merge fan-in in the low byte (2 = binary passes, 4/8/16 =
+// k-way), the binary-pass tile shape (0 = P_*, 1 = P2_*) above it. Chosen per
+// kind and size by the tuning table (capi.cu).
+inline int shape_fan(int code) { return code & 0xFF; }
+inline int shape_variant(int code) { return code >> 8; }
+inline int shape_code(int fan, int variant) { return fan | (variant << 8); }
 
 // Number of binary merge passes after K1 for runs to reach `limit` items.
 inline int merge_passes(uint64_t limit, uint64_t tile) {
@@ -133,7 +148,8 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
 // Device scratch (bytes) one sort needs: binary splits or k-way range bounds,
 // plus an error word.
 template <class T>
-uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan, uint64_t start_run = 0) {
+uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int code, uint64_t start_run = 0) {
+    const int fan = shape_fan(code);
     uint64_t bytes = merge_split_slots<T>(n) * sizeof(int64_t);
     for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), fan, start_run)) {
         if (p.fan > 2 && p.rpg > 1) {
@@ -161,12 +177,14 @@ uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int fan, uint64_t s
 // device memory.
 template <class T>
 cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint64_t sort_n, uint64_t xin,
-                             uint64_t xout, uint64_t start_run, int fan, void* scratch, cudaStream_t st,
+                             uint64_t xout, uint64_t start_run, int code, void* scratch, cudaStream_t st,
                              LaunchStats* stats) {
     using C = Config<T>;
     using KC = KwayCfg<T>;
     constexpr int T1 = k1_tile<T>();
-    constexpr int MT = merge_tile<T>();
+    const int fan = shape_fan(code);
+    const bool shape2 = shape_variant(code) == 1;
+    const int MT = shape2 ? C::P2_TILE : merge_tile<T>();
     if (n == 0) return cudaSuccess;
     const bool full = (sort_n == 0 || sort_n >= n);
     const uint64_t limit = chunk_limit(n, sort_n);
@@ -180,7 +198,7 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     const T* cur = start_run ? in : written_by(0);
     int64_t* splits = static_cast<int64_t*>(scratch);
     int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
-                                      pipeline_scratch_bytes<T>(n, sort_n, fan, start_run) - 256);
+                                      pipeline_scratch_bytes<T>(n, sort_n, code, start_run) - 256);
 
     static bool configured = false;
     if (!configured) {
@@ -192,6 +210,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
+        cudaFuncSetAttribute(pair_merge_kernel<T, C::P2_NT, C::P2_VT, C::STABLE, C::P2_TILE, C::P2_MINB>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape2<T>::SMEM);
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
         configured = true;
@@ -232,9 +252,12 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                 pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
             });
             launch(n_k3.c_str(), st, [&] {
-                pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB><<<(unsigned)tiles, C::P_NT,
-                                                                                         merge_smem<T>(), st>>>(
-                    cur, nxt, n, run, splits, xo);
+                if (shape2)
+                    pair_merge_kernel<T, C::P2_NT, C::P2_VT, C::STABLE, C::P2_TILE, C::P2_MINB>
+                        <<<(unsigned)tiles, C::P2_NT, PShape2<T>::SMEM, st>>>(cur, nxt, n, run, splits, xo);
+                else
+                    pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB>
+                        <<<(unsigned)tiles, C::P_NT, merge_smem<T>(), st>>>(cur, nxt, n, run, splits, xo);
             });
             if (stats) stats->kernels += 2;
         } else {

@@ -108,6 +108,16 @@ def lib():
         L.origami_server_reset_stats.argtypes = [vp]
         L.origami_server_destroy.restype = i
         L.origami_server_destroy.argtypes = [vp]
+        L.origami_autotune.restype = i
+        L.origami_autotune.argtypes = [i, u64, ctypes.c_char_p, u64]
+        L.origami_tuning_get.restype = i
+        L.origami_tuning_get.argtypes = [i, u64, ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.origami_tuning_set.restype = i
+        L.origami_tuning_set.argtypes = [i, u64, i, i]
+        L.origami_tuning_save.restype = i
+        L.origami_tuning_save.argtypes = [ctypes.c_char_p]
+        L.origami_tuning_load.restype = i
+        L.origami_tuning_load.argtypes = [ctypes.c_char_p]
         L.origami_generate_device.restype = i
         L.origami_generate_device.argtypes = [i, vp, u64, i, u64, vp]
         L.origami_seg_plan_create.restype = i
@@ -324,6 +334,36 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(kind, n):
+    """Time every pass shape on n device items of `kind`; the fastest becomes the
+    default for n's size class. Returns {"fan", "variant", "report"}."""
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    buf = ctypes.create_string_buffer(4096)
+    check(lib().origami_autotune(k, n, buf, len(buf)))
+    fan, var = tuning_get(k, n)
+    return {"fan": fan, "variant": var, "report": buf.value.decode()}
+
+
+def tuning_get(kind, n):
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    f, v = ctypes.c_int(), ctypes.c_int()
+    check(lib().origami_tuning_get(k, n, ctypes.byref(f), ctypes.byref(v)))
+    return f.value, v.value
+
+
+def tuning_set(kind, n, fan, variant=0):
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    check(lib().origami_tuning_set(k, n, fan, variant))
+
+
+def tuning_save(path):
+    check(lib().origami_tuning_save(os.fsencode(path)))
+
+
+def tuning_load(path):
+    check(lib().origami_tuning_load(os.fsencode(path)))
 
 
 WRITER_DISTS = {"uniform": 1, "same": 2, "sorted": 3, "reverse": 4, "almost_sorted": 5,

@@ -93,3 +93,27 @@ def test_server_without_device(lib):
     st = og.ServerStats()
     assert lib.origami_server_get_stats(None, ctypes.byref(st)) == og.ERR_INVALID
     assert lib.origami_server_destroy(None) == og.ERR_INVALID
+
+
+def test_tuning_table_roundtrip(lib, tmp_path):
+    # the table needs no device: set, read back, save, reset, load
+    for k in range(5):
+        assert og.tuning_get(k, 1 << 20) == (2, 0)  # default: binary passes, first tile shape
+    og.tuning_set(og.U32, 1 << 20, 2, 1)
+    og.tuning_set(og.KV64, 1 << 27, 8, 0)
+    assert og.tuning_get(og.U32, (1 << 21) - 1) == (2, 1)  # same size class
+    assert og.tuning_get(og.U32, 1 << 21) == (2, 0)
+    path = tmp_path / "tune.txt"
+    og.tuning_save(path)
+    lines = sorted(path.read_text().split("\n"))
+    assert "0 20 2 1" in lines and "3 27 8 0" in lines
+    og.tuning_set(og.U32, 1 << 20, 2, 0)
+    og.tuning_set(og.KV64, 1 << 27, 2, 0)
+    og.tuning_load(path)
+    assert og.tuning_get(og.U32, 1 << 20) == (2, 1) and og.tuning_get(og.KV64, 1 << 27) == (8, 0)
+    with pytest.raises(og.OrigamiError):
+        og.tuning_set(og.U32, 100, 3, 0)
+    with pytest.raises(og.OrigamiError):
+        og.tuning_set(og.U32, 100, 4, 1)  # the tile shape choice is for binary passes
+    og.tuning_set(og.U32, 1 << 20, 2, 0)
+    og.tuning_set(og.KV64, 1 << 27, 2, 0)
