@@ -3,7 +3,7 @@
 //
 // A plan owns its scratch (allocated once at creation), so a replay makes no
 // allocation and issues one graph launch instead of the memset and the
-// 3 + 2 x levels kernel launches of the plain call. This is the form for a
+// 4 + 2 x levels kernel launches of the plain call. This is the form for a
 // caller that sorts the same set of segment buffers repeatedly (a batch slot
 // refilled between calls).
 #include <mutex>

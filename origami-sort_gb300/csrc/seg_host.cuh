@@ -22,7 +22,7 @@ const SegGrids<T>& seg_grids() {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(seg_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SegShape<T>::SMEM);
         cudaFuncSetAttribute(seg_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape<T>::SMEM);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_tile_kernel<T>, SegShape<T>::NT, SegShape<T>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_tile_kernel<T>, SegShape<T>::NTM, SegShape<T>::SMEM);
         const int tile = sms * (per > 0 ? per : 1);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T>, Config<T>::P_NT, PShape<T>::SMEM);
         g.merge = sms * (per > 0 ? per : 1);
@@ -49,13 +49,15 @@ cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t 
     const unsigned b = (unsigned)((nseg + 255) / 256);
     static const std::string n_plan = std::string("seg_plan<") + TypeName<T>::v + ">";
     static const std::string n_scan = std::string("seg_scan<") + TypeName<T>::v + ">";
+    static const std::string n_fill = std::string("seg_fill<") + TypeName<T>::v + ">";
     static const std::string n_tile = std::string("seg_tile<") + TypeName<T>::v + ">";
     static const std::string n_part = std::string("seg_partition<") + TypeName<T>::v + ">";
     static const std::string n_merge = std::string("seg_merge<") + TypeName<T>::v + ">";
     launch(n_plan.c_str(), st, [&] { seg_plan_kernel<T><<<b, 256, 0, st>>>(s); });
     launch(n_scan.c_str(), st, [&] { seg_scan_kernel<T><<<(unsigned)(maxl + 1), 1024, 0, st>>>(s); });
+    launch(n_fill.c_str(), st, [&] { seg_fill_kernel<T><<<b, 256, 0, st>>>(s); });
     launch(n_tile.c_str(), st, [&] {
-        seg_tile_kernel<T><<<g.tile, SegShape<T>::NT, SegShape<T>::SMEM, st>>>(s, d, tmp, xmask);
+        seg_tile_kernel<T><<<g.tile, SegShape<T>::NTM, SegShape<T>::SMEM, st>>>(s, d, tmp, xmask);
     });
     for (int l = 0; l < maxl; ++l) {
         launch(n_part.c_str(), st, [&] { seg_part_kernel<T><<<g.part, 256, 0, st>>>(s, l, d, tmp); });

@@ -35,6 +35,7 @@ struct SegCfg<uint32_t> {
     static constexpr int NW = 8, VT = 32;  // tile: 8 warps x 32 lanes x 32 keys = 8192
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = false;
+    static constexpr int NWT = 9;  // warps in the shared-memory rounds (one merge block per thread)
     static constexpr int TILE_MINB = 3, MERGE_MINB = 8;  // CTAs per SM the register budget allows
 };
 template <>
@@ -42,6 +43,7 @@ struct SegCfg<uint64_t> {
     static constexpr int NW = 8, VT = 16;  // 4096
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = false;
+    static constexpr int NWT = 9;
     static constexpr int TILE_MINB = 2, MERGE_MINB = 8;
 };
 template <>
@@ -49,6 +51,7 @@ struct SegCfg<KV64> {
     static constexpr int NW = 8, VT = 8;  // 2048, stable block sort
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = true;
+    static constexpr int NWT = 8;
     static constexpr int TILE_MINB = 3, MERGE_MINB = 6;
 };
 
@@ -72,6 +75,7 @@ struct SegState {
     uint32_t* tot;        // [maxl+1] jobs per row
     int64_t* splits;      // merge-path split of each merge tile of the current level
     uint32_t* segof;      // segment of each merge tile of the current level
+    uint32_t* tileseg;    // segment of each tile job
     int* err;             // 2 = bad offsets
 };
 
@@ -150,11 +154,22 @@ __global__ void __launch_bounds__(1024) seg_scan_kernel(SegState st) {
     if (threadIdx.x == 1023) st.tot[blockIdx.x] = part[1023];
 }
 
+// 3. the segment of every tile job (one thread per segment)
+template <class T>
+__global__ void seg_fill_kernel(SegState st) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= st.nseg) return;
+    const SegGeom<T> g(st.off, s, st.n);
+    const uint32_t b = st.cnt[s];
+    for (uint32_t t = 0; t < g.tiles; ++t) st.tileseg[b + t] = s;
+}
+
 // ------------------------------------------------------------ tile phase --
 template <class T>
 struct SegShape {
     using C = SegCfg<T>;
-    static constexpr int NT = C::NW * 32;
+    static constexpr int NT = C::NW * 32;   // threads that load and sort in registers
+    static constexpr int NTM = C::NWT * 32; // threads of the CTA (all take part in the rounds)
     static constexpr int BUF = padded_items<T>(C::TILE + C::VT + 1);
     static constexpr size_t BUF_BYTES = (((size_t)BUF * sizeof(T)) + 15) & ~(size_t)15;
     static constexpr size_t SMEM = 2 * BUF_BYTES;
@@ -163,81 +178,93 @@ struct SegShape {
 
 // Sorts items [p0, p0+cnt) of `src` (cnt <= TILE) into `dst` at the same
 // positions: register/warp sort, then shared-memory rounds up to the tile.
+// Any alignment of p0: loads and stores are plain and coalesced.
 template <class T>
 __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64_t xin, uint64_t xout,
                               unsigned char* smem, int* split) {
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
-    constexpr int NT = Sh::NT, VT = C::VT, TILE = C::TILE, WT = 32 * VT;
+    constexpr int NT = Sh::NT, NTM = Sh::NTM, VT = C::VT, TILE = C::TILE, WT = 32 * VT;
     T* sa = reinterpret_cast<T*>(smem);
     T* sb = reinterpret_cast<T*>(smem + Sh::BUF_BYTES);
     const int tid = threadIdx.x;
-#pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const int i = k * NT + tid;
-        sa[pad<T>(i)] = (i < cnt) ? Traits<T>::flip(src[p0 + i], xin) : Traits<T>::max_item();
-    }
-    __syncthreads();
     // the sorted span: the smallest power of two >= cnt (at least one warp run)
     int span = WT;
     while (span < cnt) span <<= 1;
     if constexpr (C::STABLE) {
+#pragma unroll
+        for (int k = 0; k < VT; ++k) {
+            const int i = k * NT + tid;
+            if (tid < NT) sa[pad<T>(i)] = (i < cnt) ? Traits<T>::flip(src[p0 + i], xin) : Traits<T>::max_item();
+        }
+        __syncthreads();
         T v[VT];
+        if (tid < NT) {
 #pragma unroll
-        for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(tid * VT + k)];
-        thread_sort<T, VT, true>(v, VT);
+            for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(tid * VT + k)];
+            thread_sort<T, VT, true>(v, VT);
+        }
         __syncthreads();
+        if (tid < NT) {
 #pragma unroll
-        for (int k = 0; k < VT; ++k) sa[pad<T>(tid * VT + k)] = v[k];
+            for (int k = 0; k < VT; ++k) sa[pad<T>(tid * VT + k)] = v[k];
+        }
         __syncthreads();
-        merge_round_uniform<T, NT, VT - 1, true, PadIdx<T>>(sa, sb, VT, TILE, split);
+        merge_round_uniform<T, NTM, VT - 1, true, PadIdx<T>>(sa, sb, VT, TILE, split);
         T* s0 = sb;
         T* s1 = sa;
         for (int w = 2 * VT; w < TILE && w < span; w <<= 1) {
-            merge_round_uniform<T, NT, VT - 1, true, LinIdx>(s0, s1, w, TILE, split);
+            merge_round_uniform<T, NTM, VT - 1, true, LinIdx>(s0, s1, w, TILE, split);
             T* t = s0;
             s0 = s1;
             s1 = t;
         }
-        for (int i = tid; i < cnt; i += NT) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
+        for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
     } else {
-        const int lane = tid & 31, w0 = (tid >> 5) * WT;
-        T v[VT];
+        // each sorting warp loads its WT slots striped (one 128-byte line per
+        // instruction) straight into registers: which keys a lane starts with
+        // does not matter once the warp's run is sorted
+        const int lane = tid & 31, warp = tid >> 5, w0 = warp * WT;
+        if (warp < C::NW) {
+            T v[VT];
 #pragma unroll
-        for (int k = 0; k < VT; ++k) v[k] = sa[pad<T>(w0 + lane * VT + k)];
-        warp_sort<T, VT>(v, WT);
-        __syncwarp();
+            for (int k = 0; k < VT; ++k) {
+                const int i = w0 + k * 32 + lane;
+                v[k] = (i < cnt) ? Traits<T>::flip(src[p0 + i], xin) : Traits<T>::max_item();
+            }
+            warp_sort<T, VT>(v, WT);
 #pragma unroll
-        for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+            for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
+        }
         __syncthreads();
         if (span > WT) {
-            merge_round_uniform<T, NT, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
+            merge_round_uniform<T, NTM, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
             T* s0 = sb;
             T* s1 = sa;
             for (int w = 2 * WT; w < span; w <<= 1) {
-                merge_round_uniform<T, NT, VT, false, LinIdx>(s0, s1, w, TILE, split);
+                merge_round_uniform<T, NTM, VT, false, LinIdx>(s0, s1, w, TILE, split);
                 T* t = s0;
                 s0 = s1;
                 s1 = t;
             }
-            for (int i = tid; i < cnt; i += NT) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
+            for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
         } else {
-            for (int i = tid; i < cnt; i += NT) dst[p0 + i] = Traits<T>::flip(sa[pad<T>(i)], xout);
+            for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(sa[pad<T>(i)], xout);
         }
     }
 }
 
-// 3. tile phase: a grid of CTAs strides over the tile jobs
+// 4. tile phase: a grid of CTAs strides over the tile jobs
 template <class T>
-__global__ void __launch_bounds__(SegShape<T>::NT, SegCfg<T>::TILE_MINB) seg_tile_kernel(SegState st, T* d, T* tmp,
-                                                                                         uint64_t xmask) {
+__global__ void __launch_bounds__(SegShape<T>::NTM, SegCfg<T>::TILE_MINB) seg_tile_kernel(SegState st, T* d, T* tmp,
+                                                                                          uint64_t xmask) {
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int split[Sh::SPLITS];
     const uint32_t total = st.tot[0];
     for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
-        const uint32_t s = seg_of_job(st.cnt, st.nseg, j);
+        const uint32_t s = st.tileseg[j];
         const SegGeom<T> g(st.off, s, st.n);
         const uint32_t t = j - st.cnt[s];
         const uint64_t p0 = st.off[s] + (uint64_t)t * C::TILE;
@@ -261,7 +288,7 @@ struct SegPair {
     }
 };
 
-// 4. level l, partition: one thread per merge tile
+// 5. level l, partition: one thread per merge tile
 template <class T>
 __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
     const uint32_t* pref = st.cnt + (size_t)(1 + l) * st.nseg;
@@ -278,7 +305,7 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
     }
 }
 
-// 5. level l, merge: a grid of CTAs strides over the merge tiles
+// 6. level l, merge: a grid of CTAs strides over the merge tiles
 template <class T>
 __global__ void __launch_bounds__(Config<T>::P_NT, SegCfg<T>::MERGE_MINB) seg_merge_kernel(SegState st, int l, T* d,
                                                                                            T* tmp, uint64_t xmask) {
@@ -324,10 +351,16 @@ inline uint64_t seg_tile_slots(uint64_t n, uint64_t nseg) {
     return n / Config<T>::P_TILE + nseg + 2;  // merge tiles of one level, upper bound
 }
 
+// Tile jobs: every segment's tiles, upper bound.
+template <class T>
+inline uint64_t seg_tile_jobs(uint64_t n, uint64_t nseg) {
+    return n / SegCfg<T>::TILE + nseg + 2;
+}
+
 template <class T>
 inline uint64_t seg_scratch_bytes(uint64_t n, uint64_t nseg, int maxl) {
     const uint64_t q = (uint64_t)maxl + 1;
-    uint64_t b = 0;
+    uint64_t b = ((seg_tile_jobs<T>(n, nseg) * 4 + 255) & ~255ull);  // tileseg
     b += ((q * nseg * 4 + 255) & ~255ull);                      // cnt
     b += ((q * 4 + 255) & ~255ull);                             // tot
     b += ((seg_tile_slots<T>(n, nseg) * 8 + 255) & ~255ull);    // splits
@@ -355,6 +388,7 @@ inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64
     s.splits = reinterpret_cast<int64_t*>(take(seg_tile_slots<T>(n, nseg) * 8));
     s.segof = reinterpret_cast<uint32_t*>(take(seg_tile_slots<T>(n, nseg) * 4));
     s.err = reinterpret_cast<int*>(take(256));
+    s.tileseg = reinterpret_cast<uint32_t*>(take(seg_tile_jobs<T>(n, nseg) * 4));
     return s;
 }
 

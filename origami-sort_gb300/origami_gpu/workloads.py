@@ -105,6 +105,14 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
     seg_launches = (int(lib().origami_launch_count()) - l0) // steps
     seg_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     plan.close()
+    # per-kernel split of the same sort (outside the graph, one call)
+    from . import profile_enable, profile_report, sort_segmented
+    d.copy_(pristine)
+    torch.cuda.synchronize()
+    profile_enable(True)
+    sort_segmented(d, offs, tmp, kind=U32, stream=stream.cuda_stream)
+    kernels = {k: {"launches": c, "ms": round(ms, 3)} for k, (c, ms) in profile_report().items()}
+    profile_enable(False)
 
     # the plain single-array sort looped over the same arrays, from C-ABI calls
     L = lib()
@@ -140,7 +148,7 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
                     f"keys uniform (torch seed {seed}); {n} keys in total",
         "keys": n, "segments": nseg, "correct": ok,
         "segmented_graph_ms": seg_ms, "segmented_gkeys_s": n / seg_ms / 1e6,
-        "kernels_per_replay": seg_launches,
+        "kernels_per_replay": seg_launches, "kernels": kernels,
         "loop_plain_ms": loop_ms, "loop_plain_gkeys_s": n / loop_ms / 1e6,
         "speedup_vs_loop": loop_ms / seg_ms,
         "l2": "inputs (GBs) larger than L2; restored from a pristine copy before each step",

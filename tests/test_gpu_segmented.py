@@ -134,7 +134,7 @@ def test_segmented_graph_plan(kind):
     o = torch.from_numpy(off.astype(np.int64)).cuda()
     src = d.clone()
     plan = og.SegmentedPlan(d, o, tmp, kind=kind)
-    assert plan.kernels >= 3  # plan, scan, tile phase, then two kernels per merge level
+    assert plan.kernels >= 4  # plan, scan, fill, tile phase, then two kernels per merge level
     s = torch.cuda.current_stream().cuda_stream
     want = expected(a, off)
     for _ in range(3):  # replays over refilled input
