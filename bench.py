@@ -182,6 +182,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(torch, dist, value, device):
+    """The largest `value` over all ranks (the slowest replica sets the time)."""
+    if not dist:
+        return value
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gkeys_per_s(n, steps, world, total_ms):
+    """Whole-job rate: every replica sorts n keys per step."""
+    return world * n * steps / (total_ms / 1e3) / 1e9
+
+
 def short_workloads(torch):
     """Batched and serving measurements carried on the headline line (shorter
     runs than `--workload batched|serving`). Failures are reported, not raised."""
@@ -344,12 +358,8 @@ def main():
     report = og.profile_report()
     og.profile_enable(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * args.steps / (total_ms / 1e3) / 1e9
+    total_ms = max_over_ranks(torch, dist, sum(step_ms), dev)
+    value = job_gkeys_per_s(n, args.steps, world, total_ms)
     peak, peak_src = peaks()
     item = 4
     # dominant kernel and its roofline
