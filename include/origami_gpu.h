@@ -260,15 +260,15 @@ typedef struct origami_server_stats {
     double keys_per_s; /* keys / (last completion - first submission) */
 } origami_server_stats;
 
-int origami_server_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
+int origami_serve_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
                           uint64_t max_batch_items, uint64_t max_queue);
-int origami_server_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
+int origami_serve_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
                           uint64_t* id);
-int origami_server_wait(origami_server* s, uint64_t id, int64_t timeout_ms);
-int origami_server_cancel(origami_server* s, uint64_t id);
-int origami_server_get_stats(origami_server* s, origami_server_stats* out);
-int origami_server_reset_stats(origami_server* s);
-int origami_server_destroy(origami_server* s);
+int origami_serve_wait(origami_server* s, uint64_t id, int64_t timeout_ms);
+int origami_serve_cancel(origami_server* s, uint64_t id);
+int origami_serve_get_stats(origami_server* s, origami_server_stats* out);
+int origami_serve_reset_stats(origami_server* s);
+int origami_serve_destroy(origami_server* s);
 
 /*
  * Device-side input generator for the reference's Writer distributions

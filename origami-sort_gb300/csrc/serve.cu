@@ -355,7 +355,7 @@ struct origami_server {
 
 extern "C" {
 
-int origami_server_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
+int origami_serve_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,
                           uint64_t max_batch_items, uint64_t max_queue) {
     if (!out) return origami::api_fail(ORIGAMI_ERR_INVALID, "out is NULL");
     *out = nullptr;
@@ -372,7 +372,7 @@ int origami_server_create(origami_server** out, uint64_t hbm_budget_bytes, int m
     return ORIGAMI_OK;
 }
 
-int origami_server_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
+int origami_serve_submit(origami_server* s, int kind, const void* in, void* out, uint64_t n,
                           uint64_t* id) {
     if (!s || !id) return origami::api_fail(ORIGAMI_ERR_INVALID, "server and id are required");
     *id = 0;
@@ -421,7 +421,7 @@ int origami_server_submit(origami_server* s, int kind, const void* in, void* out
     return ORIGAMI_OK;
 }
 
-int origami_server_wait(origami_server* s, uint64_t id, int64_t timeout_ms) {
+int origami_serve_wait(origami_server* s, uint64_t id, int64_t timeout_ms) {
     if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(id);
@@ -439,7 +439,7 @@ int origami_server_wait(origami_server* s, uint64_t id, int64_t timeout_ms) {
     return ORIGAMI_OK;
 }
 
-int origami_server_cancel(origami_server* s, uint64_t id) {
+int origami_serve_cancel(origami_server* s, uint64_t id) {
     if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->reqs.find(id);
@@ -451,7 +451,7 @@ int origami_server_cancel(origami_server* s, uint64_t id) {
     return ORIGAMI_OK;
 }
 
-int origami_server_get_stats(origami_server* s, origami_server_stats* out) {
+int origami_serve_get_stats(origami_server* s, origami_server_stats* out) {
     if (!s || !out) return origami::api_fail(ORIGAMI_ERR_INVALID, "server and out are required");
     std::lock_guard<std::mutex> lk(s->mu);
     std::vector<double> l = s->lat_ms;
@@ -480,7 +480,7 @@ int origami_server_get_stats(origami_server* s, origami_server_stats* out) {
     return ORIGAMI_OK;
 }
 
-int origami_server_reset_stats(origami_server* s) {
+int origami_serve_reset_stats(origami_server* s) {
     if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat_ms.clear();
@@ -492,7 +492,7 @@ int origami_server_reset_stats(origami_server* s) {
     return ORIGAMI_OK;
 }
 
-int origami_server_destroy(origami_server* s) {
+int origami_serve_destroy(origami_server* s) {
     if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
     {
         std::lock_guard<std::mutex> lk(s->mu);

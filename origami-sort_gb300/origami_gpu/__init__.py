@@ -94,20 +94,20 @@ def lib():
         L.origami_noalloc_max_items.argtypes = [i]
         L.origami_sort_noalloc_device.restype = i
         L.origami_sort_noalloc_device.argtypes = [i, vp, vp, u64, u64, i, ctypes.POINTER(vp), vp]
-        L.origami_server_create.restype = i
-        L.origami_server_create.argtypes = [ctypes.POINTER(vp), u64, i, u64, u64]
-        L.origami_server_submit.restype = i
-        L.origami_server_submit.argtypes = [vp, i, vp, vp, u64, ctypes.POINTER(u64)]
-        L.origami_server_wait.restype = i
-        L.origami_server_wait.argtypes = [vp, u64, ctypes.c_int64]
-        L.origami_server_cancel.restype = i
-        L.origami_server_cancel.argtypes = [vp, u64]
-        L.origami_server_get_stats.restype = i
-        L.origami_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
-        L.origami_server_reset_stats.restype = i
-        L.origami_server_reset_stats.argtypes = [vp]
-        L.origami_server_destroy.restype = i
-        L.origami_server_destroy.argtypes = [vp]
+        L.origami_serve_create.restype = i
+        L.origami_serve_create.argtypes = [ctypes.POINTER(vp), u64, i, u64, u64]
+        L.origami_serve_submit.restype = i
+        L.origami_serve_submit.argtypes = [vp, i, vp, vp, u64, ctypes.POINTER(u64)]
+        L.origami_serve_wait.restype = i
+        L.origami_serve_wait.argtypes = [vp, u64, ctypes.c_int64]
+        L.origami_serve_cancel.restype = i
+        L.origami_serve_cancel.argtypes = [vp, u64]
+        L.origami_serve_get_stats.restype = i
+        L.origami_serve_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+        L.origami_serve_reset_stats.restype = i
+        L.origami_serve_reset_stats.argtypes = [vp]
+        L.origami_serve_destroy.restype = i
+        L.origami_serve_destroy.argtypes = [vp]
         L.origami_autotune.restype = i
         L.origami_autotune.argtypes = [i, u64, ctypes.c_char_p, u64]
         L.origami_tuning_get.restype = i
@@ -291,7 +291,7 @@ class Server:
 
     def __init__(self, hbm_budget_bytes=0, max_inflight=0, max_batch_items=0, max_queue=0):
         h = ctypes.c_void_p()
-        check(lib().origami_server_create(ctypes.byref(h), hbm_budget_bytes, max_inflight,
+        check(lib().origami_serve_create(ctypes.byref(h), hbm_budget_bytes, max_inflight,
                                           max_batch_items, max_queue))
         self._h = h
 
@@ -301,26 +301,26 @@ class Server:
         p, n = _ptr_len(x, k)
         q = p if out is None else _ptr_len(out, k)[0]
         rid = ctypes.c_uint64()
-        check(lib().origami_server_submit(self._h, k, p, q, n, ctypes.byref(rid)))
+        check(lib().origami_serve_submit(self._h, k, p, q, n, ctypes.byref(rid)))
         return rid.value
 
     def wait(self, rid, timeout_ms=-1):
-        check(lib().origami_server_wait(self._h, rid, timeout_ms))
+        check(lib().origami_serve_wait(self._h, rid, timeout_ms))
 
     def cancel(self, rid):
-        check(lib().origami_server_cancel(self._h, rid))
+        check(lib().origami_serve_cancel(self._h, rid))
 
     def stats(self):
         st = ServerStats()
-        check(lib().origami_server_get_stats(self._h, ctypes.byref(st)))
+        check(lib().origami_serve_get_stats(self._h, ctypes.byref(st)))
         return st.as_dict()
 
     def reset_stats(self):
-        check(lib().origami_server_reset_stats(self._h))
+        check(lib().origami_serve_reset_stats(self._h))
 
     def close(self):
         if self._h is not None and self._h.value:
-            check(lib().origami_server_destroy(self._h))
+            check(lib().origami_serve_destroy(self._h))
         self._h = None
 
     def __enter__(self):

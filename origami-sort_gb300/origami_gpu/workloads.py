@@ -213,17 +213,17 @@ def serve_rate(server, pool, rate, duration_s, seed, max_requests=None):
         j = i % len(pool.items)
         it = pool.items[j]
         if j in slot_ids:  # the output buffer is reused: its last request must be done
-            check(L.origami_server_wait(server._h, slot_ids.pop(j), -1))
+            check(L.origami_serve_wait(server._h, slot_ids.pop(j), -1))
         now = time.perf_counter()
         if t_next > now:
             time.sleep(t_next - now)
-        check(L.origami_server_submit(server._h, it["kind"], it["in"].data_ptr(), it["out"].data_ptr(),
+        check(L.origami_serve_submit(server._h, it["kind"], it["in"].data_ptr(), it["out"].data_ptr(),
                                       it["n"], ctypes.byref(rid)))
         slot_ids[j] = rid.value
         ids.append(rid.value)
         i += 1
     for r in slot_ids.values():
-        check(L.origami_server_wait(server._h, r, -1))
+        check(L.origami_serve_wait(server._h, r, -1))
     st = server.stats()
     st["offered_rate"] = rate
     st["requests"] = len(ids)
@@ -391,6 +391,36 @@ def plain_configs(torch, steps=3, warmup=2, dev=None):
         return float(np.mean(ms))
 
     out = {}
+    # 1,048,576 uint32 keys (4 MiB, L2-resident, launch-bound): device time and
+    # the host call the reference's bench_sort makes (pageable buffers)
+    n1 = 1 << 20
+    p1 = torch.randint(-(2**31), 2**31, (n1,), dtype=torch.int32, device=dev, generator=gen)
+    d1, t1 = torch.empty_like(p1), torch.empty_like(p1)
+    ms1 = []
+    for i in range(warmup + 20):
+        d1.copy_(p1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        check(L.origami_sort_device(U32, d1.data_ptr(), t1.data_ptr(), n1, 0, 0, 0, ctypes.byref(res),
+                                    ctypes.c_void_p(stream.cuda_stream)))
+        b.record(stream)
+        torch.cuda.synchronize()
+        if i >= warmup:
+            ms1.append(a.elapsed_time(b))
+    h_in = p1.cpu().numpy().view(np.uint32)
+    h = h_in.copy()
+    ht = np.empty_like(h)
+    host_ms = []
+    for i in range(warmup + 10):
+        h[:] = h_in
+        t0 = time.perf_counter()
+        check(L.origami_sort(U32, h.ctypes.data, ht.ctypes.data, n1, 0, 0, 0, ctypes.byref(res)))
+        if i >= warmup:
+            host_ms.append((time.perf_counter() - t0) * 1e3)
+    out["u32_1M"] = {"n": n1, "device_ms": float(np.median(ms1)), "device_gkeys_s": n1 / float(np.median(ms1)) / 1e6,
+                     "host_ms": float(np.median(host_ms)), "host_gkeys_s": n1 / float(np.median(host_ms)) / 1e6,
+                     "equal_to_numpy_sort": bool(np.array_equal(h, np.sort(h_in)))}
+    del p1, d1, t1
     n64 = 1 << 27
     p = torch.randint(-(2**63), 2**63 - 1, (n64,), dtype=torch.int64, device=dev, generator=gen)
     d, tmp = torch.empty_like(p), torch.empty_like(p)

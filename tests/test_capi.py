@@ -87,12 +87,12 @@ def test_server_without_device(lib):
     if torch.cuda.is_available():
         pytest.skip("a GPU is present")
     h = ctypes.c_void_p()
-    assert lib.origami_server_create(ctypes.byref(h), 0, 0, 0, 0) == og.ERR_NO_DEVICE
+    assert lib.origami_serve_create(ctypes.byref(h), 0, 0, 0, 0) == og.ERR_NO_DEVICE
     assert not h.value
-    assert lib.origami_server_create(None, 0, 0, 0, 0) == og.ERR_INVALID
+    assert lib.origami_serve_create(None, 0, 0, 0, 0) == og.ERR_INVALID
     st = og.ServerStats()
-    assert lib.origami_server_get_stats(None, ctypes.byref(st)) == og.ERR_INVALID
-    assert lib.origami_server_destroy(None) == og.ERR_INVALID
+    assert lib.origami_serve_get_stats(None, ctypes.byref(st)) == og.ERR_INVALID
+    assert lib.origami_serve_destroy(None) == og.ERR_INVALID
 
 
 def test_tuning_table_roundtrip(lib, tmp_path):

@@ -125,13 +125,13 @@ def test_oversized_and_bad_arguments():
         L = og.lib()
         import ctypes
         rid = ctypes.c_uint64()
-        assert L.origami_server_submit(s._h, 0, None, None, 10, ctypes.byref(rid)) == og.ERR_INVALID
-        assert L.origami_server_submit(s._h, 9, big.ctypes.data, None, 10, ctypes.byref(rid)) == og.ERR_DTYPE
+        assert L.origami_serve_submit(s._h, 0, None, None, 10, ctypes.byref(rid)) == og.ERR_INVALID
+        assert L.origami_serve_submit(s._h, 9, big.ctypes.data, None, 10, ctypes.byref(rid)) == og.ERR_DTYPE
         # overlapping input and output that are not the same buffer
-        assert L.origami_server_submit(s._h, 0, big.ctypes.data, big.ctypes.data + 4, 10,
+        assert L.origami_serve_submit(s._h, 0, big.ctypes.data, big.ctypes.data + 4, 10,
                                        ctypes.byref(rid)) == og.ERR_INVALID
-        assert L.origami_server_wait(s._h, 12345, 0) == og.ERR_INVALID
-        assert L.origami_server_cancel(s._h, 12345) == og.ERR_INVALID
+        assert L.origami_serve_wait(s._h, 12345, 0) == og.ERR_INVALID
+        assert L.origami_serve_cancel(s._h, 12345) == og.ERR_INVALID
         # the server still works after rejected calls
         a = make(og.U32, 1000, np.random.default_rng(1))
         x = a.copy()
