@@ -34,7 +34,7 @@ struct Config<uint32_t> {
 template <>
 struct Config<uint64_t> {
     static constexpr bool WARP_K1 = true;
-    static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 1;
+    static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 3;
     static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
     static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 8;
     static constexpr int P2_NT = 160, P2_VT = 32, P2_TILE = 4096, P2_MINB = 1;
