@@ -115,12 +115,12 @@ struct MergeTreeOps {
     using C = KwayCfg<T>;
 
     static void configure() {
-        static bool done = false;
-        if (!done) {
+        static const bool done = [] {
             cudaFuncSetAttribute(range_merge_kernel<T, StreamLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)KwayLayout<T>::SMEM);
-            done = true;
-        }
+            return true;
+        }();
+        (void)done;
     }
 
     // One pass: up to KWAY_MAX streams into dst. xin/xout: flips on read/write.

@@ -200,8 +200,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
                                       pipeline_scratch_bytes<T>(n, sort_n, code, start_run) - 256);
 
-    static bool configured = false;
-    if (!configured) {
+    // kernel attributes, once per process (thread-safe static initialisation)
+    static const bool configured = [] {
         if constexpr (C::WARP_K1)
             cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
@@ -214,8 +214,9 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape2<T>::SMEM);
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
-        configured = true;
-    }
+        return true;
+    }();
+    (void)configured;
 
     static const std::string n_k1 = std::string("block_sort<") + TypeName<T>::v + ">";
     static const std::string n_k4 = std::string("pair_partition<") + TypeName<T>::v + ">";
@@ -299,12 +300,12 @@ cudaError_t kway_pass_sliced(const T* in, T* out, uint64_t n, uint64_t run, int 
     using KC = KwayCfg<T>;
     static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
-    static bool configured = false;
-    if (!configured) {
+    static const bool configured = [] {
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
-        configured = true;
-    }
+        return true;
+    }();
+    (void)configured;
     if (n == 0) return cudaSuccess;
     const uint64_t rpg = (n + KC::RANGE - 1) / KC::RANGE;
     int64_t* bnd = static_cast<int64_t*>(scratch);

@@ -15,8 +15,8 @@ struct SegGrids {
 
 template <class T>
 const SegGrids<T>& seg_grids() {
-    static SegGrids<T> g;
-    if (g.tile == 0) {
+    static const SegGrids<T> grids = [] {  // thread-safe static initialisation
+        SegGrids<T> g;
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -28,8 +28,9 @@ const SegGrids<T>& seg_grids() {
         g.merge = sms * (per > 0 ? per : 1);
         g.part = sms * 8;
         g.tile = tile;
-    }
-    return g;
+        return g;
+    }();
+    return grids;
 }
 
 template <class T>
