@@ -44,7 +44,7 @@ template <>
 struct Config<KV64> {
     static constexpr bool WARP_K1 = false;  // key-value items need stable merges
     static constexpr int K1_NW = 8, K1_NWT = 8, K1_VT = 8, K1_MINB = 1;
-    static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 7;  // 2048 items (32 KiB)
+    static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 11;  // 2048 items (32 KiB), serial blocks of 11
     static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 1;  // serial merge blocks of 11
     static constexpr int P2_NT = 160, P2_VT = 7, P2_TILE = 1024, P2_MINB = 8;
     static constexpr bool STABLE = true;

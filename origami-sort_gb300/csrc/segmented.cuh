@@ -35,6 +35,7 @@ struct SegCfg<uint32_t> {
     static constexpr int NW = 8, VT = 32;  // tile: 8 warps x 32 lanes x 32 keys = 8192
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = false;
+    static constexpr int VTM = VT;  // (stable rounds only)
     static constexpr int NWT = 9;  // warps in the shared-memory rounds (one merge block per thread)
     static constexpr int TILE_MINB = 3, MERGE_MINB = 8;  // CTAs per SM the register budget allows
 };
@@ -43,6 +44,7 @@ struct SegCfg<uint64_t> {
     static constexpr int NW = 8, VT = 16;  // 4096
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = false;
+    static constexpr int VTM = VT;
     static constexpr int NWT = 9;
     static constexpr int TILE_MINB = 2, MERGE_MINB = 8;
 };
@@ -51,6 +53,7 @@ struct SegCfg<KV64> {
     static constexpr int NW = 8, VT = 8;  // 2048, stable block sort
     static constexpr int TILE = NW * 32 * VT;
     static constexpr bool STABLE = true;
+    static constexpr int VTM = 11;  // serial merge blocks of the shared-memory rounds
     static constexpr int NWT = 8;
     static constexpr int TILE_MINB = 3, MERGE_MINB = 6;
 };
@@ -173,7 +176,8 @@ struct SegShape {
     static constexpr int BUF = padded_items<T>(C::TILE + C::VT + 1);
     static constexpr size_t BUF_BYTES = (((size_t)BUF * sizeof(T)) + 15) & ~(size_t)15;
     static constexpr size_t SMEM = 2 * BUF_BYTES;
-    static constexpr int SPLITS = C::TILE / (C::VT - 1) + C::TILE / (2 * C::VT) + 8;
+    static constexpr int VO = C::STABLE ? C::VTM : C::VT - 1;  // outputs per merge block of the rounds
+    static constexpr int SPLITS = C::TILE / VO + C::TILE / (2 * C::VT) + 8;
 };
 
 // Sorts items [p0, p0+cnt) of `src` (cnt <= TILE) into `dst` at the same
@@ -210,11 +214,11 @@ __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
             for (int k = 0; k < VT; ++k) sa[pad<T>(tid * VT + k)] = v[k];
         }
         __syncthreads();
-        merge_round_uniform<T, NTM, VT - 1, true, PadIdx<T>>(sa, sb, VT, TILE, split);
+        merge_round_uniform<T, NTM, C::VTM, true, PadIdx<T>>(sa, sb, VT, TILE, split);
         T* s0 = sb;
         T* s1 = sa;
         for (int w = 2 * VT; w < TILE && w < span; w <<= 1) {
-            merge_round_uniform<T, NTM, VT - 1, true, LinIdx>(s0, s1, w, TILE, split);
+            merge_round_uniform<T, NTM, C::VTM, true, LinIdx>(s0, s1, w, TILE, split);
             T* t = s0;
             s0 = s1;
             s1 = t;
