@@ -339,8 +339,11 @@ uint64_t typed_scratch_io(int kind, uint64_t n, uint64_t sort_n, int fan, uint64
 }
 
 // Second compute stream and copy stream of the calling thread (host sorts).
+// Per-thread helper streams of the host pipeline: 0 .. HOST_LANES-2 sort
+// chunks beside the caller's stream, HOST_LANES-1 carries the copies.
+constexpr int HOST_LANES = 5;
 cudaStream_t aux_stream(int which) {
-    thread_local cudaStream_t s[2] = {nullptr, nullptr};
+    thread_local cudaStream_t s[HOST_LANES] = {};
     if (!s[which]) cudaStreamCreateWithFlags(&s[which], cudaStreamNonBlocking);
     return s[which];
 }
@@ -404,19 +407,25 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
     const uint64_t m = key_mask(kind);
     const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
     uint64_t chunk_n = 1ull << 22;
-    while (chunk_n * 16 <= n) chunk_n <<= 1;  // 8 to 16 chunks
+    while (chunk_n * 16 <= n) chunk_n <<= 1;  // 8 to 16 chunks (4 and 16 measured slower at 1 GiB)
     const bool chunked = shape_fan(fan) == 2 && n >= 4 * chunk_n && limit > chunk_n;
-    void *A = nullptr, *B = nullptr, *w0 = nullptr, *w1 = nullptr, *wm = nullptr;
+    void *A = nullptr, *B = nullptr, *wm = nullptr;
+    void* w[HOST_LANES] = {};
     CK(cudaMallocAsync(&A, bytes, st), "arena allocation");
     cudaError_t e = cudaMallocAsync(&B, bytes, st);
     if (!chunked) {
-        if (e == cudaSuccess) e = cudaMallocAsync(&w0, typed_scratch_io(kind, n, sort_n, fan, 0), st);
-        if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w0, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&w[0], typed_scratch_io(kind, n, sort_n, fan, 0), st);
+        if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w[0], st);
     } else {
-        const int cfan = shape_for(kind, chunk_n, min_k);  // the chunks' own tuned shape
+        // chunks sort on HOST_LANES-1 streams at once; binary passes use the
+        // one-tile-per-CTA merge shape, whose launches from the different
+        // streams interleave (one chunk's splitter searches overlap another's
+        // merges; 8 chunk sorts of 2^25 keys: 6.97 ms on 4 streams against
+        // 8.3 ms for the persistent kernels on one)
+        int cfan = shape_for(kind, chunk_n, min_k);  // the chunks' own tuned shape
+        if (shape_fan(cfan) == 2) cfan = shape_code(2, 2);
         const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, cfan, 0);
-        if (e == cudaSuccess) e = cudaMallocAsync(&w0, cs, st);
-        if (e == cudaSuccess) e = cudaMallocAsync(&w1, cs, st);
+        for (int i = 0; i < HOST_LANES - 1 && e == cudaSuccess; ++i) e = cudaMallocAsync(&w[i], cs, st);
         // the merges across chunks are one k-way pass: bound by the host link
         // it writes (1 GiB in ~5.6 ms), which hides its cost per level
         const uint64_t need = (limit + chunk_n - 1) / chunk_n;
@@ -424,7 +433,9 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
         while ((uint64_t)mfan < need && mfan < 16) mfan <<= 1;
         if (e == cudaSuccess) e = cudaMallocAsync(&wm, typed_scratch_io(kind, n, sort_n, mfan, chunk_n), st);
         const bool copy_in = is_pinned(host_in);
-        cudaStream_t s1 = aux_stream(0), sc = aux_stream(1);
+        cudaStream_t lanes[HOST_LANES - 1] = {st};
+        for (int i = 1; i < HOST_LANES - 1; ++i) lanes[i] = aux_stream(i - 1);
+        cudaStream_t sc = aux_stream(HOST_LANES - 1);
         std::vector<cudaEvent_t> evs;
         auto event_on = [&](cudaStream_t s) {
             cudaEvent_t ev;
@@ -435,14 +446,15 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
         };
         if (e == cudaSuccess) {
             const cudaEvent_t ready = event_on(st);  // buffers allocated
-            cudaStreamWaitEvent(s1, ready, 0);
+            for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(lanes[i], ready, 0);
             cudaStreamWaitEvent(sc, ready, 0);
         }
         char* a = static_cast<char*>(A);
         char* b = static_cast<char*>(B);
         for (uint64_t off = 0, c = 0; e == cudaSuccess && off < n; off += chunk_n, ++c) {
             const uint64_t cn = n - off < chunk_n ? n - off : chunk_n;
-            cudaStream_t cst = (c & 1) ? s1 : st;
+            const int lane = (int)(c % (HOST_LANES - 1));
+            cudaStream_t cst = lanes[lane];
             const void* src = static_cast<const char*>(vin) + off * ib;
             if (copy_in) {
                 e = cudaMemcpyAsync(a + off * ib, static_cast<const char*>(host_in) + off * ib, cn * ib,
@@ -451,11 +463,11 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                 src = a + off * ib;
             }
             if (e == cudaSuccess)
-                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, cfan,
-                             (c & 1) ? w1 : w0, cst);
+                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, cfan, w[lane],
+                             cst);
         }
         if (e == cudaSuccess) {
-            cudaStreamWaitEvent(st, event_on(s1), 0);
+            for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(st, event_on(lanes[i]), 0);
             if (limit == n && is_pinned(host_out)) {
                 // one k-way pass into HBM in 8 slices; each finished slice goes
                 // to the host on the copy stream while the next ones merge
@@ -478,8 +490,8 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
         for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once their work completes
     }
     if (wm) cudaFreeAsync(wm, st);
-    if (w1) cudaFreeAsync(w1, st);
-    if (w0) cudaFreeAsync(w0, st);
+    for (void* p : w)
+        if (p) cudaFreeAsync(p, st);
     if (B) cudaFreeAsync(B, st);
     cudaFreeAsync(A, st);
     const cudaError_t es = cudaStreamSynchronize(st);
@@ -496,7 +508,7 @@ int tune_load_file(const char* path) {
     while (std::fscanf(f, "%d %d %d %d", &kind, &cls, &fan, &var) == 4) {
         if (kind < 0 || kind > 4 || cls < 0 || cls >= TUNE_CLASSES) continue;
         if (fan != 2 && fan != 4 && fan != 8 && fan != 16) continue;
-        if (var < 0 || var > 1 || (fan != 2 && var != 0)) continue;
+        if (var < 0 || var > 2 || (fan != 2 && var != 0)) continue;
         g_tune[kind][cls].store(shape_code(fan, var), std::memory_order_relaxed);
         ++loaded;
     }
@@ -819,8 +831,8 @@ int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant) {
 int origami_tuning_set(int kind, uint64_t n, int fan, int variant) {
     if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
     if (fan != 2 && fan != 4 && fan != 8 && fan != 16) return fail(ORIGAMI_ERR_INVALID, "fan must be 2, 4, 8 or 16");
-    if (variant < 0 || variant > 1 || (fan != 2 && variant != 0))
-        return fail(ORIGAMI_ERR_INVALID, "variant must be 0 or 1 (1 only with fan 2)");
+    if (variant < 0 || variant > 2 || (fan != 2 && variant != 0))
+        return fail(ORIGAMI_ERR_INVALID, "variant must be 0, 1 or 2 (1 and 2 only with fan 2)");
     std::call_once(g_tune_once, tune_init);
     g_tune[kind][size_class(n)].store(shape_code(fan, variant), std::memory_order_relaxed);
     return ORIGAMI_OK;
@@ -862,7 +874,8 @@ int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap) {
     CK(cudaMallocAsync(&p, bytes, st), "autotune buffers");
     cudaError_t e = cudaMallocAsync(&d, bytes, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&t, bytes, st);
-    const int codes[] = {shape_code(2, 0), shape_code(2, 1), shape_code(4, 0), shape_code(8, 0), shape_code(16, 0)};
+    const int codes[] = {shape_code(2, 0), shape_code(2, 1), shape_code(2, 2), shape_code(4, 0), shape_code(8, 0),
+                         shape_code(16, 0)};
     uint64_t wbytes = 0;
     for (int c : codes) wbytes = std::max<uint64_t>(wbytes, scratch_bytes(kind, n, 0, c));
     if (e == cudaSuccess) e = cudaMallocAsync(&work, wbytes, st);

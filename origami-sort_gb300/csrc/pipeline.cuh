@@ -27,8 +27,12 @@ struct Config<uint32_t> {
     // 8 warps sort 1024 keys each; 9 warps share the merge rounds (265 blocks)
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 32, K1_MINB = 3;
     static constexpr int K1_NT = 256, K1_VTS = 32, K1_VTM = 32;  // (block K1, unused)
-    static constexpr int P_NT = 160, P_VT = 32, P_TILE = 4096, P_MINB = 1;  // binary pass tiles
-    static constexpr int P2_NT = 288, P2_VT = 32, P2_TILE = 8192, P2_MINB = 5;  // second tile shape
+    // binary pass tiles (P_BULK: the persistent bulk-copy merge kernel)
+    static constexpr int P_NT = 160, P_VT = 32, P_TILE = 4096, P_MINB = 6;
+    static constexpr bool P_BULK = true;
+    static constexpr int P2_NT = 288, P2_VT = 32, P2_TILE = 8192, P2_MINB = 3;  // second tile shape
+    static constexpr bool P2_BULK = true;
+    static constexpr int PI_MINB = 1;  // the first shape as one tile per CTA (variant 2)
     static constexpr bool STABLE = false;
 };
 template <>
@@ -36,8 +40,11 @@ struct Config<uint64_t> {
     static constexpr bool WARP_K1 = true;
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 3;
     static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
-    static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 8;
-    static constexpr int P2_NT = 160, P2_VT = 32, P2_TILE = 4096, P2_MINB = 1;
+    static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 6;
+    static constexpr bool P_BULK = true;
+    static constexpr int P2_NT = 288, P2_VT = 16, P2_TILE = 4096, P2_MINB = 3;
+    static constexpr bool P2_BULK = true;
+    static constexpr int PI_MINB = 8;
     static constexpr bool STABLE = false;
 };
 template <>
@@ -45,8 +52,11 @@ struct Config<KV64> {
     static constexpr bool WARP_K1 = false;  // key-value items need stable merges
     static constexpr int K1_NW = 8, K1_NWT = 8, K1_VT = 8, K1_MINB = 1;
     static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 11;  // 2048 items (32 KiB), serial blocks of 11
-    static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 1;  // serial merge blocks of 11
-    static constexpr int P2_NT = 160, P2_VT = 7, P2_TILE = 1024, P2_MINB = 8;
+    static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 4;  // serial merge blocks of 11
+    static constexpr bool P_BULK = true;
+    static constexpr int P2_NT = 192, P2_VT = 11, P2_TILE = 2048, P2_MINB = 3;
+    static constexpr bool P2_BULK = true;
+    static constexpr int PI_MINB = 1;
     static constexpr bool STABLE = true;
 };
 
@@ -74,13 +84,66 @@ constexpr size_t merge_smem() {
 }
 template <class T>
 using PShape2 = PairShape<T, Config<T>::P2_NT, Config<T>::P2_VT, Config<T>::STABLE, Config<T>::P2_TILE>;
+// One binary-pass merge shape: pair_merge_kernel (one tile per CTA, cp.async
+// staging) or, with BULK, pair_merge_bulk_kernel (persistent, double-buffered
+// bulk copies, as many CTAs as fit on the GPU at once).
+template <class T, int NT, int VT, int TILE, int MINB, bool BULK>
+struct PairMerge {
+    static constexpr bool ST = Config<T>::STABLE;
+    static constexpr size_t SMEM = BULK ? PairBulkShape<T, NT, VT, ST, TILE>::SMEM : PairShape<T, NT, VT, ST, TILE>::SMEM;
+    static void configure() {
+        if constexpr (BULK)
+            cudaFuncSetAttribute(pair_merge_bulk_kernel<T, NT, VT, ST, TILE, MINB>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+        else
+            cudaFuncSetAttribute(pair_merge_kernel<T, NT, VT, ST, TILE, MINB>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    }
+    // resident CTAs on the whole GPU (the persistent grid)
+    static uint64_t resident() {
+        static const uint64_t r = [] {
+            configure();
+            int dev = 0, sms = 0, per = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pair_merge_bulk_kernel<T, NT, VT, ST, TILE, MINB>, NT,
+                                                          SMEM);
+            return (uint64_t)sms * (uint64_t)(per > 0 ? per : 1);
+        }();
+        return r;
+    }
+    // claim: the tile counter pair_partition_kernel reset just before
+    static void launch(const T* cur, T* nxt, uint64_t n, uint64_t run, const int64_t* splits, uint64_t tiles,
+                       uint64_t xo, unsigned* claim, int* err, cudaStream_t st) {
+        if constexpr (BULK) {
+            const uint64_t g = tiles < resident() ? tiles : resident();
+            pair_merge_bulk_kernel<T, NT, VT, ST, TILE, MINB>
+                <<<(unsigned)g, NT, SMEM, st>>>(cur, nxt, n, run, splits, tiles, xo, claim, ~0u, err);
+        } else {
+            (void)claim;
+            (void)err;
+            pair_merge_kernel<T, NT, VT, ST, TILE, MINB><<<(unsigned)tiles, NT, SMEM, st>>>(cur, nxt, n, run, splits, xo);
+        }
+    }
+};
+template <class T>
+using PairMerge1 = PairMerge<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::P_TILE, Config<T>::P_MINB, Config<T>::P_BULK>;
+template <class T>
+using PairMerge2 =
+    PairMerge<T, Config<T>::P2_NT, Config<T>::P2_VT, Config<T>::P2_TILE, Config<T>::P2_MINB, Config<T>::P2_BULK>;
+// The first shape with one tile per CTA: several sorts on concurrent streams
+// interleave at CTA granularity, so one sort's latency-bound splitter searches
+// overlap another's merges (a persistent kernel holds the SMs until it drains).
+template <class T>
+using PairMergeI = PairMerge<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::P_TILE, Config<T>::PI_MINB, false>;
+
 static_assert(Config<uint32_t>::P2_TILE >= Config<uint32_t>::P_TILE && Config<uint64_t>::P2_TILE >= Config<uint64_t>::P_TILE &&
                   Config<KV64>::P2_TILE >= Config<KV64>::P_TILE,
               "the splitter array is sized by the first (smallest) tile");
 
 // A pass shape code: merge fan-in in the low byte (2 = binary passes, 4/8/16 =
-// k-way), the binary-pass tile shape (0 = P_*, 1 = P2_*) above it. Chosen per
-// kind and size by the tuning table (capi.cu).
+// k-way), the binary-pass merge shape above it (0 = P_*, 1 = P2_*, 2 = P_* one
+// tile per CTA). Chosen per kind and size by the tuning table (capi.cu).
 inline int shape_fan(int code) { return code & 0xFF; }
 inline int shape_variant(int code) { return code >> 8; }
 inline int shape_code(int fan, int variant) { return fan | (variant << 8); }
@@ -146,7 +209,7 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
 }
 
 // Device scratch (bytes) one sort needs: binary splits or k-way range bounds,
-// plus an error word.
+// plus an error word and the merge kernel's tile counter (256 bytes).
 template <class T>
 uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int code, uint64_t start_run = 0) {
     const int fan = shape_fan(code);
@@ -183,8 +246,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     using KC = KwayCfg<T>;
     constexpr int T1 = k1_tile<T>();
     const int fan = shape_fan(code);
-    const bool shape2 = shape_variant(code) == 1;
-    const int MT = shape2 ? C::P2_TILE : merge_tile<T>();
+    const int variant = shape_variant(code);
+    const int MT = variant == 1 ? C::P2_TILE : merge_tile<T>();
     if (n == 0) return cudaSuccess;
     const bool full = (sort_n == 0 || sort_n >= n);
     const uint64_t limit = chunk_limit(n, sort_n);
@@ -199,6 +262,7 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     int64_t* splits = static_cast<int64_t*>(scratch);
     int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
                                       pipeline_scratch_bytes<T>(n, sort_n, code, start_run) - 256);
+    unsigned* claim = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(err) + 64);
 
     // kernel attributes, once per process (thread-safe static initialisation)
     static const bool configured = [] {
@@ -208,10 +272,9 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         else
             cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
-        cudaFuncSetAttribute(pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem<T>());
-        cudaFuncSetAttribute(pair_merge_kernel<T, C::P2_NT, C::P2_VT, C::STABLE, C::P2_TILE, C::P2_MINB>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape2<T>::SMEM);
+        PairMerge1<T>::configure();
+        PairMerge2<T>::configure();
+        PairMergeI<T>::configure();
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
         return true;
@@ -250,15 +313,15 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
             const unsigned pblocks = (unsigned)((tiles + 1 + 255) / 256);
             const uint64_t run = p.run;
             launch(n_k4.c_str(), st, [&] {
-                pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits);
+                pair_partition_kernel<T><<<pblocks, 256, 0, st>>>(cur, n, run, MT, tiles, splits, claim);
             });
             launch(n_k3.c_str(), st, [&] {
-                if (shape2)
-                    pair_merge_kernel<T, C::P2_NT, C::P2_VT, C::STABLE, C::P2_TILE, C::P2_MINB>
-                        <<<(unsigned)tiles, C::P2_NT, PShape2<T>::SMEM, st>>>(cur, nxt, n, run, splits, xo);
+                if (variant == 1)
+                    PairMerge2<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
+                else if (variant == 2)
+                    PairMergeI<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
                 else
-                    pair_merge_kernel<T, C::P_NT, C::P_VT, C::STABLE, C::P_TILE, C::P_MINB>
-                        <<<(unsigned)tiles, C::P_NT, merge_smem<T>(), st>>>(cur, nxt, n, run, splits, xo);
+                    PairMerge1<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
             });
             if (stats) stats->kernels += 2;
         } else {

@@ -4,7 +4,10 @@
 //   K4 pair_partition_kernel  - merge-path splitter search for one binary pass
 //   K3 pair_merge_kernel      - one output tile of a binary pass, staged in
 //                               shared memory and merged by merge path
+//   K3 pair_merge_bulk_kernel - the same merge as a persistent kernel whose
+//                               tiles move by double-buffered bulk copies
 #pragma once
+#include "bulk.cuh"
 #include "common.cuh"
 #include "merge_core.cuh"
 #include "warp_sort.cuh"
@@ -215,8 +218,10 @@ struct PairGeom {
 // loads and measured slower.) splits has num_tiles+1 entries.
 template <class T>
 __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uint64_t run, int tile,
-                                      uint64_t num_tiles, int64_t* __restrict__ splits) {
+                                      uint64_t num_tiles, int64_t* __restrict__ splits,
+                                      unsigned* __restrict__ claim) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && claim) *claim = 0;  // tile counter of the merge kernel that follows
     if (t > num_tiles) return;
     const uint64_t o = t * (uint64_t)tile < n ? t * (uint64_t)tile : n;
     if (o >= n) {
@@ -288,6 +293,168 @@ __global__ void __launch_bounds__(NT, MINB) pair_merge_kernel(const T* __restric
         *reinterpret_cast<uint4*>(out + (size_t)i * V) = *reinterpret_cast<const uint4*>(tmp);
     }
     for (int i = nvec * V + tid; i < total; i += NT) out[i] = Traits<T>::flip(sout[i], xout);
+}
+
+// ------------------------------------------------------- K3, persistent ---
+// The same binary-pass merge as pair_merge_kernel, as a persistent kernel
+// whose tiles move by bulk copies (cp.async.bulk, bulk.cuh). Each CTA holds
+// two stages: while it merges the tile in one, the next tile's slices of both
+// runs are already on their way into the other, and a merged tile leaves
+// shared memory by one bulk store. Thread 0 issues every copy.
+//
+// Tiles are claimed, not assigned: a CTA starts with tile blockIdx.x and then
+// takes the next unclaimed tile from a counter (gridDim.x + atomicAdd), so CTAs
+// that became resident late (another kernel held the SMs) simply merge fewer
+// tiles. The claim for a tile is made two tiles ahead of its merge and its
+// split values are loaded one tile ahead, so neither latency is waited for.
+// *claim must be 0 at launch (pair_partition_kernel resets it).
+struct BulkTileGeom {
+    uint64_t tile;       // output tile; >= num_tiles: none (the CTA is done)
+    int as, na, bs, nb;  // A at stage[as .. as+na), B at stage[bs .. bs+nb)
+};
+
+template <class T, int NT, int VT, bool STABLE, int TILE>
+struct PairBulkShape {
+    using In = PairShape<T, NT, VT, STABLE, TILE>;
+    static constexpr size_t STAGE = (In::IN_BYTES + 127) & ~(size_t)127;
+    static constexpr size_t SMEM = 2 * STAGE;
+};
+
+// Geometry of output tile t, and the bulk loads of its slices into `stage`.
+template <class T, int TILE>
+__device__ __forceinline__ BulkTileGeom pair_bulk_issue(T* stage, const T* src, uint64_t n, uint64_t run,
+                                                        uint64_t t, int64_t s0, int64_t s1, uint64_t* bar) {
+    constexpr int V = Vec<T>::N;
+    const uint64_t o = t * TILE;
+    const PairGeom g(o, n, run);
+    const uint64_t d0 = o - g.pbase;
+    const uint64_t pair_end = g.la + g.lb;
+    const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
+    const int64_t a1 = (o + TILE < g.pbase + pair_end) ? s1 : (int64_t)g.la;
+    BulkTileGeom q;
+    q.tile = t;
+    q.na = (int)(a1 - s0);
+    q.nb = (int)(d1 - d0) - q.na;
+    const uint64_t pa = g.pbase + (uint64_t)s0;
+    const uint64_t pb = g.pbase + g.la + (d0 - (uint64_t)s0);
+    // the enclosing 16-byte vectors of each slice (never outside them)
+    const int a_lead = (int)(pa % V), b_lead = (int)(pb % V);
+    const int nva = (a_lead + q.na + V - 1) / V, nvb = (b_lead + q.nb + V - 1) / V;
+    q.as = a_lead;
+    q.bs = nva * V + b_lead;
+    mbar_arrive_expect(bar, (uint32_t)(nva + nvb) * 16u);
+    if (nva) bulk_load(stage, src + (pa - a_lead), (uint32_t)nva * 16u, bar);
+    if (nvb) bulk_load(stage + nva * V, src + (pb - b_lead), (uint32_t)nvb * 16u, bar);
+    return q;
+}
+
+template <class T, int NT, int VT, bool STABLE, int TILE, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB)
+    pair_merge_bulk_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run,
+                           const int64_t* __restrict__ splits, uint64_t num_tiles, uint64_t xout,
+                           unsigned* __restrict__ claim, unsigned max_tiles, int* err) {
+    using Sh = PairBulkShape<T, NT, VT, STABLE, TILE>;
+    constexpr int V = Vec<T>::N;
+    constexpr int VO = Block<T, VT, STABLE>::VO;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int split[Sh::In::SPLITS];
+    __shared__ BulkTileGeom geom[2];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int tid = threadIdx.x;
+    const uint64_t G = gridDim.x;
+    if (blockIdx.x >= num_tiles) return;
+    auto stage = [&](int s) { return reinterpret_cast<T*>(smem_raw + (size_t)s * Sh::STAGE); };
+    unsigned claimed = 1;  // tiles this CTA took (thread 0), at most max_tiles
+    auto claim_next = [&]() -> uint64_t {
+        if (claimed >= max_tiles) return num_tiles;
+        ++claimed;
+        return G + (uint64_t)atomicAdd(claim, 1u);
+    };
+    // thread 0's look-ahead: the next tile (with its splits) and the one after
+    uint64_t nt = num_tiles, ft = num_tiles;
+    int64_t n0 = 0, n1 = 0;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+        const uint64_t t0 = blockIdx.x;
+        geom[0] = pair_bulk_issue<T, TILE>(stage(0), src, n, run, t0, splits[t0], splits[t0 + 1], &bar[0]);
+        nt = claim_next();
+        if (nt < num_tiles) {
+            n0 = splits[nt];
+            n1 = splits[nt + 1];
+            ft = claim_next();
+        }
+    }
+    __syncthreads();
+    uint32_t phase = 0;  // bit s: parity of stage s's next completion
+    for (int s = 0;; s ^= 1) {
+        // geom[s] was written before the previous iteration's barriers
+        const BulkTileGeom q = geom[s];
+        if (q.tile >= num_tiles) break;
+        if (tid == 0) {
+            if (nt < num_tiles) {
+                bulk_wait_read<0>();  // the other stage's last store has left shared memory
+                geom[s ^ 1] = pair_bulk_issue<T, TILE>(stage(s ^ 1), src, n, run, nt, n0, n1, &bar[s ^ 1]);
+            } else {
+                geom[s ^ 1].tile = num_tiles;
+            }
+            nt = ft;
+            if (nt < num_tiles) {
+                n0 = splits[nt];
+                n1 = splits[nt + 1];
+                ft = claim_next();
+            }
+        }
+        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
+        phase ^= 1u << s;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                bulk_wait_all();
+                // the other stage's loads, if any, before shared memory goes
+                if (geom[s ^ 1].tile < num_tiles) mbar_wait(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+            }
+            return;
+        }
+        T* buf = stage(s);
+        const int total = q.na + q.nb;
+        // one merge round, outputs kept in registers until every thread has
+        // read its inputs, then written back over the stage
+        const int nblk = (total + VO - 1) / VO;
+        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
+        __syncthreads();
+        T r[VT];
+        const int diag = tid * VO;
+        const int cnt = tid < nblk ? min(VO, total - diag) : 0;
+        if (tid < nblk) {
+            const int sa = split[tid];
+            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+            merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+        }
+        __syncthreads();
+        if (cnt == VO) {
+#pragma unroll
+            for (int i = 0; i < VO; ++i) buf[diag + i] = Traits<T>::flip(r[i], xout);
+        } else {
+#pragma unroll
+            for (int i = 0; i < VO; ++i)
+                if (i < cnt) buf[diag + i] = Traits<T>::flip(r[i], xout);
+        }
+        fence_async_smem();
+        __syncthreads();
+        // output tile starts 16-byte aligned (a multiple of TILE)
+        T* out = dst + q.tile * TILE;
+        const int nvec = total / V;
+        if (tid == 0 && nvec) {
+            bulk_store(out, buf, (uint32_t)nvec * 16u);
+            bulk_commit();
+        }
+        // a ragged end (the array's last tile only, so no later tile refills
+        // this stage) is stored item by item
+        for (int i = nvec * V + tid; i < total; i += NT) out[i] = buf[i];
+    }
+    if (tid == 0) bulk_wait_read<0>();
 }
 
 }  // namespace origami
