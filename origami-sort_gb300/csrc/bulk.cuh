@@ -1,7 +1,7 @@
 // Bulk asynchronous copies between global and shared memory (the TMA unit's
 // untiled form, cp.async.bulk) and the shared-memory mbarriers that track them.
 //
-// Every wait is bounded: bulk_wait() gives up after BULK_SPIN_LIMIT polls and
+// Every wait is bounded: mbar_wait() gives up after BULK_SPIN_LIMIT polls and
 // returns false, so a kernel can record an error and leave instead of spinning
 // forever.
 #pragma once
@@ -77,5 +77,14 @@ __device__ __forceinline__ void bulk_wait_read() {
 }
 // Waits until all of this thread's bulk groups have completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
+// Programmatic dependent launch. A kernel launched with the programmatic
+// stream serialization attribute may start while the kernel before it in the
+// stream still runs; grid_dep_wait() returns once that kernel has completed and
+// its writes are visible, so a dependent kernel calls it before it touches
+// memory the previous kernel reads or writes. grid_dep_launch() lets the next
+// such kernel start launching. Both do nothing in a kernel launched normally.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
 }  // namespace origami

@@ -220,6 +220,8 @@ template <class T>
 __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uint64_t run, int tile,
                                       uint64_t num_tiles, int64_t* __restrict__ splits,
                                       unsigned* __restrict__ claim) {
+    grid_dep_launch();  // the merge kernel may take its place on the SMs early
+    grid_dep_wait();    // the previous pass's merge has finished (and read splits)
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0 && claim) *claim = 0;  // tile counter of the merge kernel that follows
     if (t > num_tiles) return;
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(NT, MINB)
     using Sh = PairBulkShape<T, NT, VT, STABLE, TILE>;
     constexpr int V = Vec<T>::N;
     constexpr int VO = Block<T, VT, STABLE>::VO;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int split[Sh::In::SPLITS];
     __shared__ BulkTileGeom geom[2];
     __shared__ __align__(8) uint64_t bar[2];
@@ -377,6 +379,14 @@ __global__ void __launch_bounds__(NT, MINB)
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_init_fence();
+    }
+    // launched as a dependent of the partition kernel: wait for its splits and
+    // counter. (The kernel does not release its own dependents early: the next
+    // partition launches as the CTAs exit. Releasing them at the start, so that
+    // they take SM slots while this grid still merges, made a 1 GiB sort 25 %
+    // slower.)
+    grid_dep_wait();
+    if (tid == 0) {
         const uint64_t t0 = blockIdx.x;
         geom[0] = pair_bulk_issue<T, TILE>(stage(0), src, n, run, t0, splits[t0], splits[t0 + 1], &bar[0]);
         nt = claim_next();
