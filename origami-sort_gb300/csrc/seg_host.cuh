@@ -21,10 +21,12 @@ const SegGrids<T>& seg_grids() {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(seg_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SegShape<T>::SMEM);
-        cudaFuncSetAttribute(seg_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PShape<T>::SMEM);
+        cudaFuncSetAttribute(seg_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)SegMergeShape<T>::SMEM);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_tile_kernel<T>, SegShape<T>::NTM, SegShape<T>::SMEM);
         const int tile = sms * (per > 0 ? per : 1);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T>, Config<T>::P_NT, PShape<T>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T>, Config<T>::P_NT,
+                                                      SegMergeShape<T>::SMEM);
         g.merge = sms * (per > 0 ? per : 1);
         g.part = sms * 8;
         g.tile = tile;
@@ -63,7 +65,7 @@ cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t 
     for (int l = 0; l < maxl; ++l) {
         launch(n_part.c_str(), st, [&] { seg_part_kernel<T><<<g.part, 256, 0, st>>>(s, l, d, tmp); });
         launch(n_merge.c_str(), st, [&] {
-            seg_merge_kernel<T><<<g.merge, Config<T>::P_NT, PShape<T>::SMEM, st>>>(s, l, d, tmp, xmask);
+            seg_merge_kernel<T><<<g.merge, Config<T>::P_NT, SegMergeShape<T>::SMEM, st>>>(s, l, d, tmp, xmask);
         });
     }
     return cudaGetLastError();

@@ -9,9 +9,10 @@
 //                registers and shared memory;
 //   level l      every segment longer than T1 << l merges its runs of
 //                T1 << l pairwise: a partition kernel finds each output tile's
-//                merge-path split, a merge kernel merges the tiles (the
-//                binary-pass merge body: shared-memory staging, output written
-//                over the input, one block per thread).
+//                merge-path split and records the tile's geometry, a
+//                persistent merge kernel merges the tiles (the binary-pass
+//                merge body with double-buffered bulk copies and claimed
+//                tiles, as pair_merge_bulk_kernel).
 // A segment with L levels alternates between d and tmp so that its last step
 // writes d: its tiles go to tmp when L is odd.
 //
@@ -37,7 +38,7 @@ struct SegCfg<uint32_t> {
     static constexpr bool STABLE = false;
     static constexpr int VTM = VT;  // (stable rounds only)
     static constexpr int NWT = 9;  // warps in the shared-memory rounds (one merge block per thread)
-    static constexpr int TILE_MINB = 3, MERGE_MINB = 8;  // CTAs per SM the register budget allows
+    static constexpr int TILE_MINB = 3;  // CTAs per SM the register budget allows
 };
 template <>
 struct SegCfg<uint64_t> {
@@ -46,7 +47,7 @@ struct SegCfg<uint64_t> {
     static constexpr bool STABLE = false;
     static constexpr int VTM = VT;
     static constexpr int NWT = 9;
-    static constexpr int TILE_MINB = 2, MERGE_MINB = 8;
+    static constexpr int TILE_MINB = 2;
 };
 template <>
 struct SegCfg<KV64> {
@@ -55,7 +56,7 @@ struct SegCfg<KV64> {
     static constexpr bool STABLE = true;
     static constexpr int VTM = 11;  // serial merge blocks of the shared-memory rounds
     static constexpr int NWT = 8;
-    static constexpr int TILE_MINB = 3, MERGE_MINB = 6;
+    static constexpr int TILE_MINB = 3;
 };
 
 // Merge levels for a segment of len items (runs of TILE doubled until one).
@@ -77,7 +78,8 @@ struct SegState {
                           // level-l merge tiles; exclusive prefixes after the scan
     uint32_t* tot;        // [maxl+1] jobs per row
     int64_t* splits;      // merge-path split of each merge tile of the current level
-    uint32_t* segof;      // segment of each merge tile of the current level
+    struct SegTileRec* rec;  // geometry of each merge tile of the current level
+    unsigned* claim;      // [maxl] tile counter of each level's merge kernel
     uint32_t* tileseg;    // segment of each tile job
     int* err;             // 2 = bad offsets
 };
@@ -182,10 +184,18 @@ struct SegShape {
 
 // Sorts items [p0, p0+cnt) of `src` (cnt <= TILE) into `dst` at the same
 // positions: register/warp sort, then shared-memory rounds up to the tile.
-// Any alignment of p0: loads and stores are plain and coalesced.
+// Any alignment of p0.
+//  - key-value items: plain coalesced loads and stores;
+//  - keys: the tile arrives by one bulk copy (the 16-byte chunks enclosing
+//    it), warps read their keys from shared memory, only the warps whose keys
+//    lie inside the sorted span (the smallest power of two >= cnt) sort, and
+//    the last round writes its output shifted by p0's misalignment so that
+//    the whole 16-byte chunks leave by one bulk store (the items before and
+//    after them directly). `bar`/`phase`: the CTA's load barrier. Returns
+//    false when a bulk-copy wait expired (err set).
 template <class T>
-__device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64_t xin, uint64_t xout,
-                              unsigned char* smem, int* split) {
+__device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64_t xin, uint64_t xout,
+                              unsigned char* smem, int* split, uint64_t* bar, uint32_t& phase, int* err) {
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
     constexpr int NT = Sh::NT, NTM = Sh::NTM, VT = C::VT, TILE = C::TILE, WT = 32 * VT;
@@ -196,6 +206,9 @@ __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
     int span = WT;
     while (span < cnt) span <<= 1;
     if constexpr (C::STABLE) {
+        (void)bar;
+        (void)phase;
+        (void)err;
 #pragma unroll
         for (int k = 0; k < VT; ++k) {
             const int i = k * NT + tid;
@@ -224,17 +237,34 @@ __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
             s1 = t;
         }
         for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
+        return true;
     } else {
-        // each sorting warp loads its WT slots striped (one 128-byte line per
-        // instruction) straight into registers: which keys a lane starts with
-        // does not matter once the warp's run is sorted
+        constexpr int V = Vec<T>::N;
         const int lane = tid & 31, warp = tid >> 5, w0 = warp * WT;
-        if (warp < C::NW) {
+        const int sh = (int)(p0 % V);  // misalignment of the tile in both buffers
+        if (tid == 0) {
+            const int nv = (sh + cnt + V - 1) / V;
+            bulk_wait_read<0>();  // the previous tile's bulk store has left shared memory
+            mbar_arrive_expect(bar, (uint32_t)nv * 16u);
+            bulk_load(sb, src + (p0 - sh), (uint32_t)nv * 16u, bar);
+        }
+        const bool ok = mbar_wait(bar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                bulk_wait_all();
+            }
+            return false;
+        }
+        if (warp < C::NW && w0 < span) {
+            // striped reads: which keys a lane starts with does not matter
+            // once the warp's run is sorted
             T v[VT];
 #pragma unroll
             for (int k = 0; k < VT; ++k) {
                 const int i = w0 + k * 32 + lane;
-                v[k] = (i < cnt) ? Traits<T>::flip(src[p0 + i], xin) : Traits<T>::max_item();
+                v[k] = (i < cnt) ? Traits<T>::flip(sb[sh + i], xin) : Traits<T>::max_item();
             }
             warp_sort<T, VT>(v, WT);
 #pragma unroll
@@ -242,19 +272,44 @@ __device__ void seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
         }
         __syncthreads();
         if (span > WT) {
-            merge_round_uniform<T, NTM, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
-            T* s0 = sb;
-            T* s1 = sa;
-            for (int w = 2 * WT; w < span; w <<= 1) {
-                merge_round_uniform<T, NTM, VT, false, LinIdx>(s0, s1, w, TILE, split);
-                T* t = s0;
+            const T* s0 = sa;
+            T* s1 = sb;
+            for (int w = WT; w < span; w <<= 1) {
+                T* out = (2 * w >= span) ? s1 + sh : s1;  // the last round writes shifted
+                if (w == WT)
+                    merge_round_uniform<T, NTM, VT, false, PadIdx<T>>(s0, out, w, span, split);
+                else
+                    merge_round_uniform<T, NTM, VT, false, LinIdx>(s0, out, w, span, split);
+                T* t = const_cast<T*>(s0);
                 s0 = s1;
                 s1 = t;
             }
-            for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(s0[i], xout);
+            T* res = const_cast<T*>(s0);  // item i at res[sh + i]
+            if (xout) {
+                for (int i = tid; i < cnt; i += NTM) res[sh + i] = Traits<T>::flip(res[sh + i], xout);
+            }
+            fence_async_smem();
+            __syncthreads();
+            T* op = dst + (p0 - sh);  // 16-byte aligned
+            const int x0 = sh ? V : 0;
+            const int x1 = ((sh + cnt) / V) * V;
+            if (x1 > x0) {
+                if (tid == 0) {
+                    bulk_store(op + x0, res + x0, (uint32_t)(x1 - x0) * (uint32_t)sizeof(T));
+                    bulk_commit();
+                }
+                const int head = x0 - sh, tail = sh + cnt - x1;
+                if (tid < head)
+                    op[sh + tid] = res[sh + tid];
+                else if (tid < head + tail)
+                    op[x1 + tid - head] = res[x1 + tid - head];
+            } else {
+                for (int i = tid; i < cnt; i += NTM) op[sh + i] = res[sh + i];
+            }
         } else {
             for (int i = tid; i < cnt; i += NTM) dst[p0 + i] = Traits<T>::flip(sa[pad<T>(i)], xout);
         }
+        return true;
     }
 }
 
@@ -266,17 +321,26 @@ __global__ void __launch_bounds__(SegShape<T>::NTM, SegCfg<T>::TILE_MINB) seg_ti
     using Sh = SegShape<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int split[Sh::SPLITS];
+    __shared__ __align__(8) uint64_t bar;
     const uint32_t total = st.tot[0];
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
     for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
         const uint32_t s = st.tileseg[j];
         const SegGeom<T> g(st.off, s, st.n);
         const uint32_t t = j - st.cnt[s];
         const uint64_t p0 = st.off[s] + (uint64_t)t * C::TILE;
         const int cnt = (int)min((uint64_t)C::TILE, g.len - (uint64_t)t * C::TILE);
-        seg_tile_sort<T>(d, seg_buf<T>(g.levels, 0, d, tmp), p0, cnt, xmask, g.levels == 0 ? xmask : 0, smem_raw,
-                         split);
+        if (!seg_tile_sort<T>(d, seg_buf<T>(g.levels, 0, d, tmp), p0, cnt, xmask, g.levels == 0 ? xmask : 0,
+                              smem_raw, split, &bar, phase, st.err))
+            return;
         __syncthreads();
     }
+    if (threadIdx.x == 0) bulk_wait_read<0>();
 }
 
 // Geometry of merge tile u (MT outputs) of a segment of len items at level l.
@@ -292,61 +356,200 @@ struct SegPair {
     }
 };
 
+// What the merge kernel needs of one merge tile, recorded by the partition
+// kernel: the pair's first item, the tile's output range within the pair, the
+// A run length and four flags in its top bits.
+struct SegTileRec {
+    uint64_t base, d0, d1, la_flags;
+    static constexpr uint64_t SRC_TMP = 1ull << 60, DST_TMP = 1ull << 61, LAST = 1ull << 62, PAIR_END = 1ull << 63;
+    static constexpr uint64_t LA_MASK = (1ull << 60) - 1;
+};
+
 // 5. level l, partition: one thread per merge tile
 template <class T>
 __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
     const uint32_t* pref = st.cnt + (size_t)(1 + l) * st.nseg;
     const uint32_t total = st.tot[1 + l];
     const uint64_t run = (uint64_t)SegCfg<T>::TILE << l;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st.claim[l] = 0;  // for this level's merge kernel
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < total;
          j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t s = seg_of_job(pref, st.nseg, (uint32_t)j);
         const SegGeom<T> g(st.off, s, st.n);
         const SegPair p(g.len, run, j - pref[s], Config<T>::P_TILE);
-        const T* A = seg_buf<const T>(g.levels, l, d, tmp) + st.off[s] + p.pb;
+        const uint64_t base = st.off[s] + p.pb;
+        const T* A = seg_buf<const T>(g.levels, l, d, tmp) + base;
         st.splits[j] = global_merge_path(A, (int64_t)p.la, A + p.la, (int64_t)p.lb, (int64_t)p.d0);
-        st.segof[j] = s;
+        uint64_t f = p.la;
+        if (seg_buf<const T>(g.levels, l, d, tmp) == tmp) f |= SegTileRec::SRC_TMP;
+        if (seg_buf<const T>(g.levels, l + 1, d, tmp) == tmp) f |= SegTileRec::DST_TMP;
+        if ((uint32_t)l + 1 == g.levels) f |= SegTileRec::LAST;
+        if (p.d1 == p.la + p.lb) f |= SegTileRec::PAIR_END;
+        SegTileRec r;
+        r.base = base;
+        r.d0 = p.d0;
+        r.d1 = p.d1;
+        r.la_flags = f;
+        st.rec[j] = r;
     }
 }
 
-// 6. level l, merge: a grid of CTAs strides over the merge tiles
+// 6. level l, merge: persistent, double-buffered bulk copies, claimed tiles
+// (the body of pair_merge_bulk_kernel). Segments start anywhere, so an output
+// tile is generally not 16-byte aligned: the merged tile is written back into
+// the stage shifted by the output's misalignment, the whole 16-byte chunks
+// leave by one bulk store and the few items before and after them are stored
+// directly from registers.
+struct SegBulkGeom {
+    uint64_t job, obase;     // job >= total: none
+    int as, na, bs, nb, sh;  // A at stage[as..), B at stage[bs..); output shift
+    uint64_t flags;
+};
+
 template <class T>
-__global__ void __launch_bounds__(Config<T>::P_NT, SegCfg<T>::MERGE_MINB) seg_merge_kernel(SegState st, int l, T* d,
-                                                                                           T* tmp, uint64_t xmask) {
+__device__ __forceinline__ SegBulkGeom seg_bulk_issue(T* stage, const T* d, const T* tmp, uint64_t j,
+                                                      const SegTileRec& r, int64_t s0, int64_t s1, uint64_t* bar) {
+    constexpr int V = Vec<T>::N;
+    const uint64_t la = r.la_flags & SegTileRec::LA_MASK;
+    const int64_t a1 = (r.la_flags & SegTileRec::PAIR_END) ? (int64_t)la : s1;
+    SegBulkGeom q;
+    q.job = j;
+    q.flags = r.la_flags;
+    q.na = (int)(a1 - s0);
+    q.nb = (int)(r.d1 - r.d0) - q.na;
+    q.obase = r.base + r.d0;
+    q.sh = (int)(q.obase % V);
+    const T* src = (r.la_flags & SegTileRec::SRC_TMP) ? tmp : d;
+    const uint64_t pa = r.base + (uint64_t)s0;
+    const uint64_t pb = r.base + la + (r.d0 - (uint64_t)s0);
+    const int a_lead = (int)(pa % V), b_lead = (int)(pb % V);
+    const int nva = (a_lead + q.na + V - 1) / V, nvb = (b_lead + q.nb + V - 1) / V;
+    q.as = a_lead;
+    q.bs = nva * V + b_lead;
+    mbar_arrive_expect(bar, (uint32_t)(nva + nvb) * 16u);
+    if (nva) bulk_load(stage, src + (pa - a_lead), (uint32_t)nva * 16u, bar);
+    if (nvb) bulk_load(stage + nva * V, src + (pb - b_lead), (uint32_t)nvb * 16u, bar);
+    return q;
+}
+
+template <class T>
+using SegMergeShape = PairBulkShape<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::STABLE, Config<T>::P_TILE>;
+
+template <class T>
+__global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_kernel(SegState st, int l, T* d,
+                                                                                       T* tmp, uint64_t xmask) {
     using C = Config<T>;
-    using Sh = PShape<T>;
-    constexpr int NT = C::P_NT, V = Sh::V;
+    using Sh = SegMergeShape<T>;
+    constexpr int V = Vec<T>::N;
+    constexpr int VO = Block<T, C::P_VT, C::STABLE>::VO;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int split[Sh::SPLITS];
-    T* sin = reinterpret_cast<T*>(smem_raw);
+    __shared__ int split[Sh::In::SPLITS];
+    __shared__ SegBulkGeom geom[2];
+    __shared__ __align__(8) uint64_t bar[2];
     const int tid = threadIdx.x;
-    const uint32_t* pref = st.cnt + (size_t)(1 + l) * st.nseg;
-    const uint32_t total = st.tot[1 + l];
-    const uint64_t run = (uint64_t)SegCfg<T>::TILE << l;
-    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
-        const uint32_t s = st.segof[j];
-        const SegGeom<T> g(st.off, s, st.n);
-        const SegPair p(g.len, run, j - pref[s], C::P_TILE);
-        const T* src = seg_buf<T>(g.levels, l, d, tmp);
-        T* dst = seg_buf<T>(g.levels, l + 1, d, tmp);
-        const uint64_t base = st.off[s] + p.pb;
-        const int64_t a0 = st.splits[j];
-        const int64_t a1 = (p.d1 < p.la + p.lb) ? st.splits[j + 1] : (int64_t)p.la;  // next tile, same pair
-        const int na = (int)(a1 - a0);
-        const int tot = (int)(p.d1 - p.d0);
-        const int nb = tot - na;
-        const int a_lead = stage_vec<T, NT>(sin, src, base + (uint64_t)a0, na);
-        const int b_base = ((a_lead + na + V - 1) / V) * V;
-        const int b_lead = stage_vec<T, NT>(sin + b_base, src, base + p.la + (p.d0 - (uint64_t)a0), nb);
-        cp_async_commit_all();
-        cp_async_wait_all();
-        __syncthreads();
-        merge_pair_round_inplace<T, NT, C::P_VT, C::STABLE>(sin, a_lead, na, b_base + b_lead, nb, split);
-        const uint64_t xo = ((uint32_t)l + 1 == g.levels) ? xmask : 0;
-        T* op = dst + base + p.d0;  // any alignment: plain coalesced stores
-        for (int i = tid; i < tot; i += NT) op[i] = Traits<T>::flip(sin[i], xo);
-        __syncthreads();
+    const uint64_t total = st.tot[1 + l];
+    const uint64_t G = gridDim.x;
+    if (blockIdx.x >= total) return;
+    unsigned* claim = st.claim + l;
+    auto stage = [&](int s) { return reinterpret_cast<T*>(smem_raw + (size_t)s * Sh::STAGE); };
+    auto claim_next = [&] { return G + (uint64_t)atomicAdd(claim, 1u); };
+    // thread 0's look-ahead: the next job (its record and splits) and the one after
+    uint64_t nj = total, fj = total;
+    SegTileRec nr{};
+    int64_t n0 = 0, n1 = 0;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+        const uint64_t j0 = blockIdx.x;
+        geom[0] = seg_bulk_issue<T>(stage(0), d, tmp, j0, st.rec[j0], st.splits[j0], st.splits[j0 + 1], &bar[0]);
+        nj = claim_next();
+        if (nj < total) {
+            nr = st.rec[nj];
+            n0 = st.splits[nj];
+            n1 = st.splits[nj + 1];
+            fj = claim_next();
+        }
     }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int s = 0;; s ^= 1) {
+        const SegBulkGeom q = geom[s];
+        if (q.job >= total) break;
+        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
+        phase ^= 1u << s;
+        if (__syncthreads_or(!ok)) {
+            // no copy into the other stage is in flight yet in this iteration
+            if (tid == 0) {
+                atomicExch(st.err, 1);
+                bulk_wait_all();
+            }
+            return;
+        }
+        // every thread is past the previous tile's stores from the other
+        // stage: thread 0 refills it with the next tile
+        if (tid == 0) {
+            if (nj < total) {
+                bulk_wait_read<0>();
+                geom[s ^ 1] = seg_bulk_issue<T>(stage(s ^ 1), d, tmp, nj, nr, n0, n1, &bar[s ^ 1]);
+            } else {
+                geom[s ^ 1].job = total;
+            }
+            nj = fj;
+            if (nj < total) {
+                nr = st.rec[nj];
+                n0 = st.splits[nj];
+                n1 = st.splits[nj + 1];
+                fj = claim_next();
+            }
+        }
+        T* buf = stage(s);
+        const int tot = q.na + q.nb;
+        const int nblk = (tot + VO - 1) / VO;
+        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
+        __syncthreads();
+        T r[C::P_VT];
+        const int diag = tid * VO;
+        const int cnt = tid < nblk ? min(VO, tot - diag) : 0;
+        if (tid < nblk) {
+            const int sa = split[tid];
+            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+        }
+        __syncthreads();
+        // stage index x holds output item x - sh, so x = 0 lies on a 16-byte
+        // boundary of the output buffer
+        const uint64_t xo = (q.flags & SegTileRec::LAST) ? xmask : 0;
+        T* w = buf + q.sh + diag;
+        if (cnt == VO) {
+#pragma unroll
+            for (int i = 0; i < VO; ++i) w[i] = Traits<T>::flip(r[i], xo);
+        } else {
+#pragma unroll
+            for (int i = 0; i < VO; ++i)
+                if (i < cnt) w[i] = Traits<T>::flip(r[i], xo);
+        }
+        fence_async_smem();
+        __syncthreads();
+        // whole 16-byte chunks [x0, x1) by one bulk store, the items before
+        // and after them directly
+        T* dst = (q.flags & SegTileRec::DST_TMP) ? tmp : d;
+        T* op = dst + q.obase - q.sh;
+        const int x0 = q.sh ? V : 0;
+        const int x1 = ((q.sh + tot) / V) * V;
+        if (x1 > x0) {
+            if (tid == 0) {
+                bulk_store(op + x0, buf + x0, (uint32_t)(x1 - x0) * (uint32_t)sizeof(T));
+                bulk_commit();
+            }
+            const int head = x0 - q.sh, tail = q.sh + tot - x1;
+            if (tid < head) op[q.sh + tid] = buf[q.sh + tid];
+            else if (tid < head + tail) op[x1 + tid - head] = buf[x1 + tid - head];
+        } else {
+            for (int i = tid; i < tot; i += C::P_NT) op[q.sh + i] = buf[q.sh + i];
+        }
+    }
+    if (tid == 0) bulk_wait_read<0>();
 }
 
 // ------------------------------------------------------------ scratch ----
@@ -368,8 +571,9 @@ inline uint64_t seg_scratch_bytes(uint64_t n, uint64_t nseg, int maxl) {
     b += ((q * nseg * 4 + 255) & ~255ull);                      // cnt
     b += ((q * 4 + 255) & ~255ull);                             // tot
     b += ((seg_tile_slots<T>(n, nseg) * 8 + 255) & ~255ull);    // splits
-    b += ((seg_tile_slots<T>(n, nseg) * 4 + 255) & ~255ull);    // segof
+    b += ((seg_tile_slots<T>(n, nseg) * sizeof(SegTileRec) + 255) & ~255ull);  // rec
     b += 256;                                                   // err
+    b += ((q * 4 + 255) & ~255ull);                             // claim
     return b;
 }
 
@@ -390,9 +594,10 @@ inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64
     s.cnt = reinterpret_cast<uint32_t*>(take(q * nseg * 4));
     s.tot = reinterpret_cast<uint32_t*>(take(q * 4));
     s.splits = reinterpret_cast<int64_t*>(take(seg_tile_slots<T>(n, nseg) * 8));
-    s.segof = reinterpret_cast<uint32_t*>(take(seg_tile_slots<T>(n, nseg) * 4));
+    s.rec = reinterpret_cast<SegTileRec*>(take(seg_tile_slots<T>(n, nseg) * sizeof(SegTileRec)));
     s.err = reinterpret_cast<int*>(take(256));
     s.tileseg = reinterpret_cast<uint32_t*>(take(seg_tile_jobs<T>(n, nseg) * 4));
+    s.claim = reinterpret_cast<unsigned*>(take(q * 4));
     return s;
 }
 
