@@ -36,8 +36,9 @@ sys.path.insert(0, os.path.join(REPO, "origami-sort_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 N_KEYS = 1 << 28
-# ncu dram__bytes_read.sum + dram__bytes_write.sum per key merged (u32 pass)
-TRAFFIC_PER_KEY = {"pair_merge": (268.596480e6 + 219.109120e6) / (1 << 26)}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum per key merged (u32 pass of
+# the persistent bulk-copy merge kernel over 2^26 keys)
+TRAFFIC_PER_KEY = {"pair_merge": (268.610304e6 + 212.318464e6) / (1 << 26)}
 METRIC = "Gkeys/s sorting 1 GB uint32 on 1 GB300 (% HBM roofline); batched p50/p99 latency"
 WORKLOAD = "full sort of 268,435,456 uint32 keys (1 GiB), uniform over [0, 2^32)"
 
@@ -372,7 +373,7 @@ def main():
                  if name.startswith(("block_sort", "pair_merge", "kway_merge"))) // args.steps
     ms_step = total_ms / args.steps
     # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
-    # capture (profiles/pair_merge_u32_64M.md: 256 MiB launch, scaled by the
+    # capture (profiles/pair_merge_bulk_u32_kv64_64M.md: 256 MiB launch, scaled by the
     # keys merged); the write count misses lines still dirty in L2 at the end
     traffic = None
     per_key = TRAFFIC_PER_KEY.get(dom_name.split("<")[0])
