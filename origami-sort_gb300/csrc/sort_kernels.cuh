@@ -213,9 +213,10 @@ struct PairGeom {
 
 // ---------------------------------------------------------------- K4 -----
 // One thread per output-tile boundary: the merge-path split (items taken from
-// the left run) at the tile's first output, by binary search. (Searches with
-// more probes per step, by one thread or a whole warp, issue more random
-// loads and measured slower.) splits has num_tiles+1 entries.
+// the left run) at the tile's first output: a few interpolation probes, then
+// binary search (common.cuh). (Searches with more probes per step, by one
+// thread or a whole warp, issue more random loads and measured slower.)
+// splits has num_tiles+1 entries.
 template <class T>
 __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uint64_t run, int tile,
                                       uint64_t num_tiles, int64_t* __restrict__ splits,
@@ -232,7 +233,7 @@ __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uin
     }
     const PairGeom g(o, n, run);
     const T* A = src + g.pbase;
-    splits[t] = global_merge_path(A, (int64_t)g.la, A + g.la, (int64_t)g.lb, (int64_t)(o - g.pbase));
+    splits[t] = global_merge_path_interp(A, (int64_t)g.la, A + g.la, (int64_t)g.lb, (int64_t)(o - g.pbase));
 }
 
 // ---------------------------------------------------------------- K3 -----
