@@ -185,12 +185,14 @@ __device__ __forceinline__ int64_t global_merge_path(const T* A, int64_t na, con
 // at most four extra probes. The split is the first i with g(i) > 0 (A[i] >
 // B[diag-1-i]: equal keys go to A first); every decision is an exact integer
 // compare, g (in float) only places probes.
+// `interp` off: plain bisection (data that fits in L2, where each bisection
+// step is a short L2 hit and the interpolation arithmetic does not pay).
 template <class T>
 __device__ __forceinline__ int64_t global_merge_path_interp(const T* A, int64_t na, const T* B, int64_t nb,
-                                                            int64_t diag) {
+                                                            int64_t diag, bool interp = true) {
     int64_t lo = diag - nb > 0 ? diag - nb : 0;
     int64_t hi = diag < na ? diag : na;
-    if (hi - lo >= 4096) {
+    if (interp && hi - lo >= 4096) {
         const auto al = Traits<T>::key(A[lo]), bl = Traits<T>::key(B[diag - 1 - lo]);
         const auto ar = Traits<T>::key(A[hi - 1]), br = Traits<T>::key(B[diag - hi]);
         if (al > bl) return lo;     // the split is lo

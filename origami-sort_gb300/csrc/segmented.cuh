@@ -379,7 +379,8 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
         const SegPair p(g.len, run, j - pref[s], Config<T>::P_TILE);
         const uint64_t base = st.off[s] + p.pb;
         const T* A = seg_buf<const T>(g.levels, l, d, tmp) + base;
-        st.splits[j] = global_merge_path_interp(A, (int64_t)p.la, A + p.la, (int64_t)p.lb, (int64_t)p.d0);
+        st.splits[j] = global_merge_path_interp(A, (int64_t)p.la, A + p.la, (int64_t)p.lb, (int64_t)p.d0,
+                                                st.n * sizeof(T) > (64ull << 20));
         uint64_t f = p.la;
         if (seg_buf<const T>(g.levels, l, d, tmp) == tmp) f |= SegTileRec::SRC_TMP;
         if (seg_buf<const T>(g.levels, l + 1, d, tmp) == tmp) f |= SegTileRec::DST_TMP;

@@ -233,7 +233,8 @@ __global__ void pair_partition_kernel(const T* __restrict__ src, uint64_t n, uin
     }
     const PairGeom g(o, n, run);
     const T* A = src + g.pbase;
-    splits[t] = global_merge_path_interp(A, (int64_t)g.la, A + g.la, (int64_t)g.lb, (int64_t)(o - g.pbase));
+    const bool interp = n * sizeof(T) > (64ull << 20);  // arrays larger than about half of L2
+    splits[t] = global_merge_path_interp(A, (int64_t)g.la, A + g.la, (int64_t)g.lb, (int64_t)(o - g.pbase), interp);
 }
 
 // ---------------------------------------------------------------- K3 -----
