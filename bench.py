@@ -422,7 +422,10 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
                      "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
                      "traffic": traffic,
-                     "pipeline_frac": (2 * n * item * passes / (ms_step / 1e3) / 1e9) / peak},
+                     "pipeline_frac": (2 * n * item * passes / (ms_step / 1e3) / 1e9) / peak,
+                     # one read + write of the array at peak (P = 1), and all passes
+                     "pass_floor_ms": 2 * n * item / (peak * 1e9) * 1e3,
+                     "passes_floor_ms": 2 * n * item * passes / (peak * 1e9) * 1e3},
         "kernels": {k: {"launches": c, "ms": ms} for k, (c, ms) in report.items()},
         "gpu_launches": launches,
         "tuning": tuning,

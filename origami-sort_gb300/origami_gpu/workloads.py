@@ -114,6 +114,8 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
     kernels = {k: {"launches": c, "ms": round(ms, 3)} for k, (c, ms) in profile_report().items()}
     profile_enable(False)
 
+    cpu = cpu_segments(pristine, off, lens, target_keys=1 << 26)
+
     # the plain single-array sort looped over the same arrays, from C-ABI calls
     L = lib()
     res = ctypes.c_void_p()
@@ -151,8 +153,38 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
         "kernels_per_replay": seg_launches, "kernels": kernels,
         "loop_plain_ms": loop_ms, "loop_plain_gkeys_s": n / loop_ms / 1e6,
         "speedup_vs_loop": loop_ms / seg_ms,
+        "cpu_segments": cpu,
         "l2": "inputs (GBs) larger than L2; restored from a pristine copy before each step",
     }
+
+
+def cpu_segments(pristine, off, lens, target_keys):
+    """Host comparator for the batched form (not the reference, which has no
+    batched form): numpy's sort of each array on all host cores, over the first
+    arrays up to target_keys keys."""
+    import concurrent.futures
+    import os
+    k = int(np.searchsorted(off, target_keys, side="right")) - 1
+    k = max(1, min(k, len(lens)))
+    host = pristine[: int(off[k])].cpu().numpy().view(np.uint32)
+    threads = os.cpu_count() or 1
+    segs = [(int(off[i]), int(off[i + 1])) for i in range(k)]
+
+    def work(idx):
+        for i in idx:
+            a, b = segs[i]
+            np.sort(host[a:b], kind="quicksort")
+
+    parts = [list(range(t, k, threads)) for t in range(threads)]
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, parts))  # warm-up
+        t0 = time.perf_counter()
+        list(ex.map(work, parts))
+        dt = time.perf_counter() - t0
+    keys = int(off[k])
+    return {"gkeys_s": keys / dt / 1e9, "threads": threads, "arrays": k, "keys": keys,
+            "sample": f"the first {k} arrays ({keys} keys), numpy sort per array, {threads} host threads; "
+                      "not the reference (it has no batched form)"}
 
 
 # ------------------------------------------------------------------ serving --
