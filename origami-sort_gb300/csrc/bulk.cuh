@@ -57,6 +57,12 @@ __device__ __forceinline__ void bulk_load(void* smem, const void* gmem, uint32_t
         : "memory");
 }
 
+// Asks the copy engine to bring `bytes` (a multiple of 16; 16-byte aligned
+// address) of global memory into L2; nothing waits for it.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* gmem, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
+
 // Orders this thread's generic shared-memory writes before later bulk copies
 // that read (or overwrite) the same bytes.
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }

@@ -310,13 +310,34 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
+    // the tile sort prefetches into L2 the tile one wave of resident CTAs
+    // further on (input in device memory only; 1 GiB: 1.89 -> 1.82 ms)
+    uint32_t ahead = 0;
+    if constexpr (C::WARP_K1) {  // (the key-value tile sort measured no gain)
+        static const uint32_t wave = [] {
+            int dev = 0, sms = 0, per = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per, warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>, C::K1_NWT * 32,
+                k1_smem<T>());
+            return (uint32_t)(sms * (per > 0 ? per : 1));
+        }();
+        if (!start_run && tiles1 > wave) {
+            cudaPointerAttributes pa;
+            if (cudaPointerGetAttributes(&pa, in) != cudaSuccess)
+                cudaGetLastError();  // not a CUDA pointer (pageable host memory): no prefetch
+            else if (pa.type == cudaMemoryTypeDevice)
+                ahead = wave;
+        }
+    }
     if (!start_run) {
         T* k1_out = written_by(0);
         launch(n_k1.c_str(), st, [&] {
             if constexpr (C::WARP_K1)
                 warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
                     <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
-                                                                             passes == 0 ? xout : 0);
+                                                                             passes == 0 ? xout : 0, ahead);
             else
                 block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>
                     <<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,

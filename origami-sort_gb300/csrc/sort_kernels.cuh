@@ -106,11 +106,14 @@ struct WarpSortShape {
     static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
 };
 
+// `ahead` > 0: the CTA first asks for the tile `ahead` places further on to be
+// brought into L2 (the tile a CTA of the next wave will load), so that later
+// CTAs find their keys in L2.
 template <class T, int NW, int VT, int NWT = NW, int MINB = 1>
 __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T* __restrict__ in,
                                                                         T* __restrict__ out, uint64_t n,
                                                                         int chunk, uint64_t xin,
-                                                                        uint64_t xout) {
+                                                                        uint64_t xout, uint32_t ahead = 0) {
     using Sh = WarpSortShape<T, NW, VT, NWT>;
     static_assert(NWT >= NW, "the sorting warps take part in the merge rounds");
     constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
@@ -124,6 +127,10 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
     static_assert(VT % Vec<T>::N == 0, "lanes load whole vectors");
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const int w0 = warp * WT;
+    if (ahead && tid == 0) {
+        const uint64_t pb = base + (uint64_t)ahead * TILE;
+        if (pb + TILE <= n) bulk_prefetch_l2(in + pb, (uint32_t)(TILE * sizeof(T)));
+    }
 
     // each lane loads VT keys with 16-byte vector loads; a partial tail is
     // filled with the largest key. When a chunk spans the warp's whole run the
