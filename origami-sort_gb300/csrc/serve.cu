@@ -9,7 +9,8 @@
 //    segmented sort's scratch) and fewer than `max_inflight` batches are on the
 //    device. The oldest request that does not fit waits until running batches
 //    finish and return their memory; nothing overtakes it.
-//  * coalescing: admitted requests of one kind form a batch. Their items are
+//  * coalescing: admitted requests of one kind and of comparable size (within a
+//    factor SIZE_RATIO of the batch's first) form a batch. Their items are
 //    copied back to back into one arena block and sorted by one segmented
 //    launch, each request a segment.
 //  * overlap: each in-flight batch has its own stream. The copies and sort of a
@@ -54,6 +55,9 @@ struct Request {
     int status = ORIGAMI_OK;
     Clock::time_point t_submit, t_done;
 };
+
+// Largest size ratio between requests of one batch (the first and each other).
+constexpr uint64_t SIZE_RATIO = 64;
 
 uint64_t item_bytes(int kind) { return kind == ORIGAMI_U32 ? 4u : (kind <= ORIGAMI_I64 ? 8u : 16u); }
 uint64_t r256(uint64_t b) { return (b + 255) & ~255ull; }
@@ -169,6 +173,12 @@ struct origami_server {
                 continue;
             }
             if (!b->reqs.empty() && items + r->n > max_batch_items) break;
+            // requests of very different sizes go to different batches: a
+            // small request batched with a huge one would wait for all of it
+            if (!b->reqs.empty()) {
+                const uint64_t h = b->reqs.front()->n, m = r->n;
+                if (m > SIZE_RATIO * h + 1024 || h > SIZE_RATIO * m + 1024) break;
+            }
             // the oldest request waits for memory rather than being overtaken,
             // so a large request is never starved by a stream of small ones
             if (in_use + need(r->kind, items + r->n, b->reqs.size() + 1) > budget) break;
