@@ -354,10 +354,11 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         const uint64_t xo = pi + 1 == passes ? xout : 0;
         if (p.fan == 2) {
             const uint64_t tiles = (n + MT - 1) / MT;
-            const unsigned pblocks = (unsigned)((tiles + 1 + 255) / 256);
+            // small blocks spread the latency-bound searches over more SMs
+            const unsigned pblocks = (unsigned)((tiles + 1 + 63) / 64);
             const uint64_t run = p.run;
             launch(n_k4.c_str(), st, [&] {
-                launch_dependent(pair_partition_kernel<T>, dim3(pblocks), dim3(256), 0, st, cur, n, run, MT, tiles,
+                launch_dependent(pair_partition_kernel<T>, dim3(pblocks), dim3(64), 0, st, cur, n, run, MT, tiles,
                                  splits, claim);
             });
             launch(n_k3.c_str(), st, [&] {
