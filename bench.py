@@ -215,7 +215,8 @@ def short_workloads(torch):
     except Exception as e:
         out["kv_distributions"] = {"error": repr(e)}
     try:
-        sv = wl.serving(torch, rates=(100, 200, 400), duration_s=2.0, pool_size=64)
+        # one rate, long enough for a steady p99 (the rate sweep is --workload serving)
+        sv = wl.serving(torch, rates=(400,), duration_s=5.0, pool_size=64)
         out["serving"] = sv
         ok = [r for r in sv["rates"] if r["failed"] == 0]
         if ok:
