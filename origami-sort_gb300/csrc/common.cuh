@@ -139,42 +139,10 @@ __device__ __forceinline__ void thread_sort(T (&v)[VT], int chunk) {
 }
 
 // Merge path (Odeh et al., "Merge Path - parallel merging made simple") over two
-// sorted lists held in padded shared memory: A = s[a0 .. a0+na), B = s[b0 .. b0+nb).
-// Returns how many of the first `diag` merged items come from A. A wins ties,
-// which makes every merge stable (A is always the earlier run).
-template <class T>
-__device__ __forceinline__ int smem_merge_path(const T* s, int a0, int na, int b0, int nb, int diag) {
-    int lo = max(0, diag - nb);
-    int hi = min(diag, na);
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const T a = s[pad<T>(a0 + mid)];
-        const T b = s[pad<T>(b0 + diag - 1 - mid)];
-        if (!less(b, a))
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
-// The same search over global memory (used by the pass partition kernels).
-template <class T>
-__device__ __forceinline__ int64_t global_merge_path(const T* A, int64_t na, const T* B, int64_t nb,
-                                                     int64_t diag) {
-    int64_t lo = diag - nb > 0 ? diag - nb : 0;
-    int64_t hi = diag < na ? diag : na;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (!less(B[diag - 1 - mid], A[mid]))
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
-// The same split with a few interpolation steps first. When the bracket is
+// sorted lists in global memory, A[0 .. na) and B[0 .. nb): how many of the
+// first `diag` merged items come from A, A winning ties (every merge is stable:
+// A is always the earlier run). Used by the pass partition kernels, with a few
+// interpolation steps before the bisection. When the bracket is
 // wide (late passes: runs of millions of items), the two ends are probed
 // together and up to three probes are placed by linear interpolation of
 // g(i) = key(A[i]) - key(B[diag-1-i]), which rises with i; bisection finishes
@@ -225,69 +193,6 @@ __device__ __forceinline__ int64_t global_merge_path_interp(const T* A, int64_t 
             hi = mid;
     }
     return lo;
-}
-
-// Loads of data that other CTAs of the same launch wrote must bypass L1 (it is
-// not coherent across SMs): ld.global.cg reads through L2 only.
-template <class T>
-__device__ __forceinline__ T ld_cg(const T* p) {
-    if constexpr (sizeof(T) == 4) {
-        return (T)__ldcg(reinterpret_cast<const unsigned int*>(p));
-    } else if constexpr (sizeof(T) == 8) {
-        return (T)__ldcg(reinterpret_cast<const unsigned long long*>(p));
-    } else {
-        const ulonglong2 q = __ldcg(reinterpret_cast<const ulonglong2*>(p));
-        T r;
-        r.key = q.x;
-        r.value = q.y;
-        return r;
-    }
-}
-
-// Merge-path split of the merged pair (A, B) at diagonal `diag`, by one warp:
-// 32 probes per step narrow the window 33-fold (few dependent loads).
-template <class T>
-__device__ int64_t warp_merge_path(const T* A, int64_t na, const T* B, int64_t nb, int64_t diag) {
-    const int lane = threadIdx.x & 31;
-    int64_t lo = diag - nb > 0 ? diag - nb : 0;
-    int64_t hi = diag < na ? diag : na;
-    // predicate P(i): A[i] <= B[diag-1-i]  (true -> the split is > i); monotone
-    while (hi - lo > 32) {
-        const int64_t step = (hi - lo) / 33;
-        const int64_t i = lo + (lane + 1) * step;
-        const bool p = !less(ld_cg(B + (diag - 1 - i)), ld_cg(A + i));
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, p);
-        const int c = __popc(m);  // probes 0..c-1 true
-        const int64_t nlo = c ? lo + c * step + 1 : lo;
-        const int64_t nhi = (c < 32) ? lo + (c + 1) * step : hi;
-        lo = nlo;
-        hi = nhi;
-    }
-    const int64_t i = lo + lane;
-    const bool p = (i < hi) && !less(ld_cg(B + (diag - 1 - i)), ld_cg(A + i));
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, p);
-    return lo + __popc(m);
-}
-
-// Serial merge of VT outputs from A = s[ia..aEnd) and B = s[ib..bEnd) (padded
-// shared memory), A first on ties. One shared-memory load per output, selected
-// by predicate rather than a branch. Reads at most one item past either end.
-template <class T, int VT>
-__device__ __forceinline__ void smem_serial_merge(const T* s, int ia, int aEnd, int ib, int bEnd,
-                                                  T (&out)[VT]) {
-    T a = s[pad<T>(ia)];
-    T b = s[pad<T>(ib)];
-#pragma unroll
-    for (int k = 0; k < VT; ++k) {
-        const bool takeA = (ib >= bEnd) || (ia < aEnd && !less(b, a));
-        out[k] = takeA ? a : b;
-        if (k + 1 < VT) {
-            const int nxt = takeA ? ++ia : ++ib;
-            const T v = s[pad<T>(nxt)];
-            a = takeA ? v : a;
-            b = takeA ? b : v;
-        }
-    }
 }
 
 // 16-byte vector view of items (all buffers the kernels touch are 16-byte

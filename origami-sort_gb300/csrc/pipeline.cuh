@@ -79,12 +79,6 @@ constexpr size_t k1_smem() {
 }
 template <class T>
 using PShape = PairShape<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::STABLE, Config<T>::P_TILE>;
-template <class T>
-constexpr size_t merge_smem() {
-    return PShape<T>::SMEM;
-}
-template <class T>
-using PShape2 = PairShape<T, Config<T>::P2_NT, Config<T>::P2_VT, Config<T>::STABLE, Config<T>::P2_TILE>;
 // Launch of a kernel that may start before the previous kernel in the stream
 // has finished (programmatic dependent launch): the kernel itself waits for it
 // (grid_dep_wait) before it touches memory, so only the launch latency and the
