@@ -469,11 +469,12 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
         if (e == cudaSuccess) {
             for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(st, event_on(lanes[i]), 0);
             if (limit == n && is_pinned(host_out)) {
-                // one k-way pass into HBM in 8 slices; each finished slice goes
-                // to the host on the copy stream while the next ones merge
+                // one k-way pass into HBM in 16 slices; each finished slice goes
+                // to the host on the copy stream while the next ones merge (at
+                // 1 GiB, 8 slices finish 0.1-0.2 ms later and 32 about 1 ms later)
                 SliceCopy sc_ctx{st, sc, static_cast<const char*>(B), static_cast<char*>(host_out), ib, &evs,
                                  cudaSuccess};
-                e = typed_kway_final(kind, A, B, n, chunk_n, mfan, m, wm, st, 8, &SliceCopy::on, &sc_ctx);
+                e = typed_kway_final(kind, A, B, n, chunk_n, mfan, m, wm, st, 16, &SliceCopy::on, &sc_ctx);
                 if (e == cudaSuccess) e = sc_ctx.e;
                 cudaStreamWaitEvent(st, event_on(sc), 0);  // B is freed on st after the copies
             } else {
