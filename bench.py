@@ -408,8 +408,8 @@ def main():
                "h2d_bytes_per_step": n * item, "d2h_bytes_per_step": n * item,
                "ms_per_step": 1e3 * statistics.mean(ts), "steps": len(ts), "correct": e2e_ok,
                "ms_each": [round(1e3 * x, 3) for x in ts],
-               # single calls on a shared host occasionally stall (host-memory
-               # traffic of other jobs); the value above keeps them, this not
+               # single calls occasionally take 1.5-4x as long on these shared
+               # hosts; the value above includes them, this one does not
                "value_median_call": n / statistics.median(ts) / 1e9}
 
     cpu = None
