@@ -399,8 +399,9 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
 // (the body of pair_merge_bulk_kernel). Segments start anywhere, so an output
 // tile is generally not 16-byte aligned: the merged tile is written back into
 // the stage shifted by the output's misalignment, the whole 16-byte chunks
-// leave by one bulk store and the few items before and after them are stored
-// directly from registers.
+// leave by one bulk store and single threads store the few items before and
+// after them. Thread 0 refills the other stage only after the iteration's
+// first barrier, when every thread is past the previous tile's stores from it.
 struct SegBulkGeom {
     uint64_t job, obase;     // job >= total: none
     int as, na, bs, nb, sh;  // A at stage[as..), B at stage[bs..); output shift
