@@ -362,11 +362,12 @@ bool is_pinned(const void* p) {
 //    pipeline whose first kernel reads the host input and whose last pass
 //    writes the host output, with the passes in between in two arena buffers.
 //  * Large sorts: the input is cut into chunks of chunk_n (a power of two,
-//    about n/8). Each chunk arrives in HBM (a copy-engine transfer for pinned
-//    memory, else the first kernel's own reads) and is sorted on one of two
-//    compute streams while the next chunk is in flight; the merge passes
-//    across chunks follow, the last of them writing the host output. The host
-//    link then carries each byte once each way, overlapped with the chunk sorts.
+//    8 to 16 chunks). Each chunk arrives in HBM (a copy-engine transfer for
+//    pinned memory, else the first kernel's own reads) and is sorted on one of
+//    four compute streams while the next chunks are in flight; one k-way pass
+//    across the chunks follows, cut into output slices that go to pinned host
+//    output while the next slices merge (or writing the host output directly).
+//    The host link carries each byte once each way, overlapped with the sorts.
 cudaError_t typed_kway_final(int kind, const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
                              void* scratch, cudaStream_t st, int slices, void (*cb)(void*, uint64_t, uint64_t),
                              void* ctx) {
