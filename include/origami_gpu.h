@@ -123,9 +123,12 @@ int origami_merge_series_device(int kind, void* src, void* dst, uint64_t n, uint
  * the chunked sort of bench_sort_phases.cpp:1307-1425 to arbitrary, uneven
  * chunks). Segment s is items [offsets[s], offsets[s+1]) of d; every segment
  * is sorted independently and in place (the result is in d; tmp is scratch of
- * n items). One persistent launch with a device work queue does all segments:
- * short ones wholly in registers or shared memory, long ones through tile
- * sorts and merge levels. Key-value segments are sorted stably.
+ * n items). All segments go through the same short launch sequence, planned
+ * on the device (no host synchronisation, so it can be captured in a CUDA
+ * graph): one tile-sort launch for every segment's tiles (a short segment is
+ * one tile, sorted in registers and shared memory), then for each merge level
+ * a partition and a persistent merge launch over the segments still merging.
+ * Key-value segments are sorted stably.
  *   _device: d, tmp, offsets are device memory, d and tmp 16-byte aligned,
  *            offsets[nseg] == n, asynchronous on `stream`
  *            (ORIGAMI_FLAG_SYNC waits and reports device-side errors:
