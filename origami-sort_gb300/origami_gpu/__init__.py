@@ -354,6 +354,10 @@ def tuning_get(kind, n):
 
 
 def tuning_set(kind, n, fan, variant=0):
+    """Pass shape for n's size class: fan 2 (binary passes) with merge shape
+    variant 0 or 1 (the persistent merge's two tile shapes) or 2 (one tile per
+    CTA, for sorts running on several streams at once); fan 4, 8 or 16 (k-way
+    passes, variant 0)."""
     k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
     check(lib().origami_tuning_set(k, n, fan, variant))
 
