@@ -36,9 +36,6 @@ sys.path.insert(0, os.path.join(REPO, "origami-sort_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 N_KEYS = 1 << 28
-# ncu dram__bytes_read.sum + dram__bytes_write.sum per key merged (u32 pass of
-# the persistent bulk-copy merge kernel over 2^26 keys)
-TRAFFIC_PER_KEY = {"pair_merge": (268.610304e6 + 212.318464e6) / (1 << 26)}
 METRIC = "Gkeys/s sorting 1 GB uint32 on 1 GB300 (% HBM roofline); batched p50/p99 latency"
 WORKLOAD = "full sort of 268,435,456 uint32 keys (1 GiB), uniform over [0, 2^32)"
 
@@ -126,7 +123,26 @@ def cpu_baseline(n_full, seconds=12.0):
     best = min(times)
     return {"value": n / best / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
             "sample": f"{n} uniform uint32 keys (1/{n_full // n} of the workload), "
-                      f"oracle sort_multi_thread restatement, min_k=16, best of {len(times)} runs"}
+                      f"oracle sort_multi_thread restatement, min_k=16, best of {len(times)} runs",
+            "reference_x86": reference_x86()}
+
+
+def reference_x86():
+    """The reference's own AVX2 / AVX-512 multi-threaded builds timed on an x86
+    host (they do not build on this Arm host): oracle/reference_x86.json, written
+    by oracle/time_reference.py. Quoted, not measured in this run."""
+    p = os.path.join(REPO, "oracle", "reference_x86.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    out = {}
+    for r in d.get("runs", []):
+        if "mkeys_s_best" in r:
+            out[r["variant"]] = {"gkeys_s": r["mkeys_s_best"] / 1e3, "threads": r["threads"],
+                                 "min_k": r["min_k"], "n": r["n"], "cpu": r["cpu"], "cores": r["cores"],
+                                 "mhz": r["mhz"], "correct": r["equal_to_numpy_sort"]}
+    return out or None
 
 
 def run_reference(args):
@@ -373,13 +389,8 @@ def main():
     passes = sum(c for name, (c, _) in report.items()
                  if name.startswith(("block_sort", "pair_merge", "kway_merge"))) // args.steps
     ms_step = total_ms / args.steps
-    # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
-    # capture (profiles/pair_merge_bulk_u32_kv64_64M.md: 256 MiB launch, scaled by the
-    # keys merged); the write count misses lines still dirty in L2 at the end
+    # DRAM bytes per launch need an ncu capture, which this run does not make
     traffic = None
-    per_key = TRAFFIC_PER_KEY.get(dom_name.split("<")[0])
-    if per_key is not None:
-        traffic = per_key * n
 
     e2e = None
     if args.e2e_steps > 0:

@@ -79,6 +79,11 @@ unsigned origami_item_bytes(int kind);
  *   result   receives d or tmp.
  * The call returns after the result is in place (host) or is enqueued on the
  * default stream (device pointers; add ORIGAMI_FLAG_SYNC to wait).
+ * Errors found on the device are reported by the calls that wait for the sort
+ * (host buffers, and device buffers with ORIGAMI_FLAG_SYNC): ORIGAMI_ERR_TIMEOUT
+ * when a merge kernel's bounded wait for a bulk copy expired (the output is then
+ * incomplete). The reference has no such error (ReportError, commons.h:103-104,
+ * prints and exits).
  */
 int origami_sort_u32(void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k, int flags,
                      void** result);
@@ -198,6 +203,18 @@ int origami_profile_report(char* buf, uint64_t cap);
 uint64_t origami_launch_count(void);
 
 /*
+ * Bound of every device-side wait (no counterpart in the reference, whose
+ * sorts never wait on a device): the polls a merge kernel makes on a bulk copy's
+ * mbarrier before it gives up, drains its own copies, records the expiry in the
+ * sort's error word and returns, so that a stalled copy ends the kernel instead
+ * of hanging the GPU. Default 2^20 polls. Read when a sort is launched (a
+ * segmented plan keeps the value it was created with). 0 makes every first
+ * wait expire: that is how the tests exercise the expiry path.
+ */
+uint32_t origami_get_wait_limit(void);
+int origami_set_wait_limit(uint32_t polls);
+
+/*
  * Allocation-free sort (no counterpart in the reference, which never needs
  * device memory). For callers that cannot allocate device memory during the
  * call: code running while another allocator holds the GPU's free memory, code
@@ -211,10 +228,12 @@ uint64_t origami_launch_count(void);
  *     same result-buffer convention and flags as origami_sort_device.
  *   - n must not exceed origami_noalloc_max_items(kind) (ORIGAMI_ERR_INVALID
  *     otherwise); binary merge passes are used (min_k = 2).
- *   - The first call on a device looks up the array's device address; make it
- *     before capturing this call into a CUDA graph.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture begins.
  *   - All calls share the one array: calls whose work overlaps on the GPU race
  *     and must be serialized by the caller.
+ *   - With ORIGAMI_FLAG_SYNC the call also reads the sort's device error word
+ *     (ORIGAMI_ERR_TIMEOUT when a merge kernel's bounded wait expired).
  */
 #define ORIGAMI_NOALLOC_SPLIT_SLOTS 524288
 uint64_t origami_noalloc_max_items(int kind);

@@ -1,15 +1,25 @@
 // Bulk asynchronous copies between global and shared memory (the TMA unit's
 // untiled form, cp.async.bulk) and the shared-memory mbarriers that track them.
 //
-// Every wait is bounded: mbar_wait() gives up after BULK_SPIN_LIMIT polls and
-// returns false, so a kernel can record an error and leave instead of spinning
-// forever.
+// Every wait is bounded: mbar_wait() gives up after a number of polls (the
+// kernel's `spin` argument, BULK_SPIN_LIMIT by default) and returns false, so a
+// kernel can record an error and leave instead of spinning forever. A kernel
+// whose wait expired drains its own copies with the full limit before it
+// returns (bulk_drain), so that no bulk load lands in shared memory that a
+// later CTA owns.
+//
+// Error words written by the kernels (int, 0 = no error):
+//   1  a bulk-copy wait expired; the copies it waited for were drained
+//   3  a bulk-copy wait expired and a drain wait expired too: copies may still
+//      have been in flight when the CTA returned
 #pragma once
 #include <cstdint>
 
 namespace origami {
 
 constexpr uint32_t BULK_SPIN_LIMIT = 1u << 20;
+constexpr int ERR_WAIT_EXPIRED = 1;
+constexpr int ERR_WAIT_UNDRAINED = 3;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -32,10 +42,10 @@ __device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, uint32_t bytes
 }
 
 // Polls the barrier until the phase with the given parity has completed;
-// false when it has not after BULK_SPIN_LIMIT polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// false when it has not after `limit` polls (0: gives up at once).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = BULK_SPIN_LIMIT) {
     const uint32_t a = smem_u32(bar);
-    for (uint32_t i = 0; i < BULK_SPIN_LIMIT; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -83,6 +93,22 @@ __device__ __forceinline__ void bulk_wait_read() {
 }
 // Waits until all of this thread's bulk groups have completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
+// Error path of a CTA whose wait on a bulk load expired (thread 0, the thread
+// that issued every copy of the CTA): records ERR_WAIT_EXPIRED, waits for its
+// bulk stores, then for each barrier in `bars` whose load is outstanding
+// (`pending` bit i set) waits with the full limit for the phase `parity` bit i.
+// If one of those waits expires as well, records ERR_WAIT_UNDRAINED.
+template <int NB>
+__device__ __forceinline__ void bulk_drain(int* err, uint64_t* bars, uint32_t pending, uint32_t parity) {
+    atomicMax(err, ERR_WAIT_EXPIRED);
+    bulk_wait_all();
+    bool drained = true;
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+        if ((pending >> i) & 1u) drained = mbar_wait(&bars[i], (parity >> i) & 1u) && drained;
+    if (!drained) atomicMax(err, ERR_WAIT_UNDRAINED);
+}
 
 // Programmatic dependent launch. A kernel launched with the programmatic
 // stream serialization attribute may start while the kernel before it in the

@@ -66,6 +66,9 @@ void prof_end(int slot, cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
     cudaEventRecord(g_recs[slot].b, st);
 }
+std::atomic<uint32_t> g_wait_limit{BULK_SPIN_LIMIT};
+uint32_t wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+
 uint64_t scratch_bytes(int kind, uint64_t n, uint64_t sort_n, int fan) {
     switch (kind) {
         case ORIGAMI_U32: return scratch_bytes_u32(n, sort_n, fan);
@@ -97,6 +100,41 @@ int cuda_fail(cudaError_t e, const char* what) {
         return fail(ORIGAMI_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
     return fail(ORIGAMI_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+
+// Device error words (bulk.cuh) of the sorts a call enqueues, copied into
+// pinned host memory behind each sort; read once the stream has drained.
+// Slots come from a per-thread pinned block in stack order, so a watch made
+// inside another (a nested call) takes the slots after the outer one's.
+constexpr int ERR_SLOTS = 256;
+thread_local int* t_err_host = nullptr;
+thread_local int t_err_top = 0;
+
+struct ErrWatch {
+    int base, top;
+    ErrWatch() : base(t_err_top), top(t_err_top) {
+        if (!t_err_host && cudaHostAlloc(&t_err_host, ERR_SLOTS * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            t_err_host = nullptr;
+        }
+    }
+    ~ErrWatch() { t_err_top = base; }
+    ErrWatch(const ErrWatch&) = delete;
+    ErrWatch& operator=(const ErrWatch&) = delete;
+    // Enqueues the copy of the error word at dev_err (device memory) on st.
+    cudaError_t watch(const void* dev_err, cudaStream_t st) {
+        if (!t_err_host || top >= ERR_SLOTS) return cudaSuccess;  // no slot left: not watched
+        int* h = t_err_host + top++;
+        t_err_top = top;
+        *h = 0;
+        return cudaMemcpyAsync(h, dev_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    }
+    // After the streams have drained: true when a watched sort timed out.
+    bool timed_out() const {
+        for (int i = base; i < top; ++i)
+            if (t_err_host && err_word_timeout(t_err_host[i])) return true;
+        return false;
+    }
+};
 
 #define CK(call, what)                                   \
     do {                                                 \
@@ -235,9 +273,12 @@ cudaError_t run_typed(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n,
     }
 }
 
-// Device-resident sort; the caller has validated the arguments.
+// Device-resident sort; the caller has validated the arguments. `watch`
+// (optional) collects the sort's device error word; with ORIGAMI_FLAG_SYNC and
+// no outer watch the call checks it itself and returns ORIGAMI_ERR_TIMEOUT
+// when a bounded wait of a merge kernel expired.
 int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, unsigned min_k,
-                     int flags, void** result, cudaStream_t st) {
+                     int flags, void** result, cudaStream_t st, ErrWatch* watch = nullptr) {
     const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
     if (in_tmp && !tmp) return fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
     // device kernels move whole items with vector loads and cp.async
@@ -265,15 +306,20 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
         }
         void* r = nullptr;
         int rc = ORIGAMI_OK;
+        ErrWatch local;
+        ErrWatch* w = watch ? watch : &local;
         e0 = cudaMemcpyAsync(ad, d, bytes, cudaMemcpyDeviceToDevice, st);
-        if (e0 == cudaSuccess) rc = sort_device_impl(kind, ad, at, n, sort_n, min_k, 0, &r, st);
+        if (e0 == cudaSuccess) rc = sort_device_impl(kind, ad, at, n, sort_n, min_k, 0, &r, st, w);
         if (e0 == cudaSuccess && rc == ORIGAMI_OK)
             e0 = cudaMemcpyAsync(in_tmp ? tmp : d, r, bytes, cudaMemcpyDeviceToDevice, st);
         cudaFreeAsync(ad, st);
         cudaFreeAsync(at, st);
         if (rc != ORIGAMI_OK) return rc;
         if (e0 != cudaSuccess) return cuda_fail(e0, "aligned staging copy");
-        if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
+        if (flags & ORIGAMI_FLAG_SYNC) {
+            CK(cudaStreamSynchronize(st), "stream sync");
+            if (!watch && local.timed_out()) return fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
+        }
         return ORIGAMI_OK;
     }
     void* scratch = nullptr;
@@ -286,10 +332,18 @@ int sort_device_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, 
         return cuda_fail(e, "splitter allocation");
     }
     e = run_typed(kind, d, tmp ? tmp : scratch, n, sort_n, in_tmp ? tmp : d, fan, work, st);
+    // the pipeline's error word: the last 256 bytes of its scratch
+    ErrWatch local;
+    ErrWatch* w = watch ? watch : ((flags & ORIGAMI_FLAG_SYNC) ? &local : nullptr);
+    if (e == cudaSuccess && w)
+        e = w->watch(static_cast<char*>(work) + scratch_bytes(kind, n, sort_n, fan) - 256, st);
     cudaFreeAsync(work, st);
     if (scratch) cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(e, "sort launch");
-    if (flags & ORIGAMI_FLAG_SYNC) CK(cudaStreamSynchronize(st), "stream sync");
+    if (flags & ORIGAMI_FLAG_SYNC) {
+        CK(cudaStreamSynchronize(st), "stream sync");
+        if (!watch && local.timed_out()) return fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
+    }
     return ORIGAMI_OK;
 }
 
@@ -379,6 +433,16 @@ cudaError_t typed_kway_final(int kind, const void* in, void* out, uint64_t n, ui
     }
 }
 
+// Byte offset of the error word in kway_pass_sliced's scratch.
+uint64_t typed_kway_final_err(int kind, uint64_t n) {
+    switch (kind) {
+        case ORIGAMI_U32: return kway_final_err_u32(n);
+        case ORIGAMI_U64:
+        case ORIGAMI_I64: return kway_final_err_u64(n);
+        default: return kway_final_err_kv(n);
+    }
+}
+
 // Copies each finished slice of the final pass to the host on the copy stream.
 struct SliceCopy {
     cudaStream_t st, sc;
@@ -412,11 +476,14 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
     const bool chunked = shape_fan(fan) == 2 && n >= 4 * chunk_n && limit > chunk_n;
     void *A = nullptr, *B = nullptr, *wm = nullptr;
     void* w[HOST_LANES] = {};
+    ErrWatch watch;  // every sort's error word, read after the final sync
     CK(cudaMallocAsync(&A, bytes, st), "arena allocation");
     cudaError_t e = cudaMallocAsync(&B, bytes, st);
     if (!chunked) {
-        if (e == cudaSuccess) e = cudaMallocAsync(&w[0], typed_scratch_io(kind, n, sort_n, fan, 0), st);
+        const uint64_t ws = typed_scratch_io(kind, n, sort_n, fan, 0);
+        if (e == cudaSuccess) e = cudaMallocAsync(&w[0], ws, st);
         if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w[0], st);
+        if (e == cudaSuccess) e = watch.watch(static_cast<char*>(w[0]) + ws - 256, st);
     } else {
         // chunks sort on HOST_LANES-1 streams at once; binary passes use the
         // one-tile-per-CTA merge shape, whose launches from the different
@@ -466,6 +533,9 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
             if (e == cudaSuccess)
                 e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, cfan, w[lane],
                              cst);
+            // the lane's next chunk sort clears the word again: read it now
+            if (e == cudaSuccess)
+                e = watch.watch(static_cast<char*>(w[lane]) + typed_scratch_io(kind, cn, 0, cfan, 0) - 256, cst);
         }
         if (e == cudaSuccess) {
             for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(st, event_on(lanes[i]), 0);
@@ -477,6 +547,7 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                                  cudaSuccess};
                 e = typed_kway_final(kind, A, B, n, chunk_n, mfan, m, wm, st, 16, &SliceCopy::on, &sc_ctx);
                 if (e == cudaSuccess) e = sc_ctx.e;
+                if (e == cudaSuccess) e = watch.watch(static_cast<char*>(wm) + typed_kway_final_err(kind, n), st);
                 cudaStreamWaitEvent(st, event_on(sc), 0);  // B is freed on st after the copies
             } else {
                 // merges from runs of chunk_n (one pass unless more than 16
@@ -487,6 +558,8 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                 void* wa = ((passes - 1) & 1) ? B : A;
                 void* wb = ((passes - 1) & 1) ? A : B;
                 e = typed_io(kind, A, vout, wa, wb, n, sort_n, 0, m, chunk_n, mfan, wm, st);
+                if (e == cudaSuccess)
+                    e = watch.watch(static_cast<char*>(wm) + typed_scratch_io(kind, n, sort_n, mfan, chunk_n) - 256, st);
             }
         }
         for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once their work completes
@@ -499,6 +572,7 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
     const cudaError_t es = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "host sort");
     if (es != cudaSuccess) return cuda_fail(es, "stream sync");
+    if (watch.timed_out()) return fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
     return ORIGAMI_OK;
 }
 
@@ -551,9 +625,10 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
     }
     int rc = ORIGAMI_OK;
     void* dres = nullptr;
+    ErrWatch watch;
     e = cudaMemcpyAsync(dd, d, bytes, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        rc = sort_device_impl(kind, dd, dt, n, sort_n, min_k, 0, &dres, st);
+        rc = sort_device_impl(kind, dd, dt, n, sort_n, min_k, 0, &dres, st, &watch);
         if (rc == ORIGAMI_OK) e = cudaMemcpyAsync(out, dres, bytes, cudaMemcpyDeviceToHost, st);
     }
     cudaFreeAsync(dd, st);
@@ -562,6 +637,7 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
     if (rc != ORIGAMI_OK) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "host staging copy");
     if (es != cudaSuccess) return cuda_fail(es, "stream sync");
+    if (watch.timed_out()) return fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
     return ORIGAMI_OK;
 }
 
@@ -708,7 +784,7 @@ int origami_sort_segmented_device(int kind, void* d, void* tmp, const uint64_t* 
     }
     cudaFreeAsync(scratch, st);
     if (e != cudaSuccess) return cuda_fail(e, "segmented sort");
-    if (herr == 1) return fail(ORIGAMI_ERR_TIMEOUT, "a merge job waited past its budget");
+    if (err_word_timeout(herr)) return fail(ORIGAMI_ERR_TIMEOUT, "a merge job waited past its budget");
     if (herr == 2) return fail(ORIGAMI_ERR_INVALID, "segment offsets decrease");
     return ORIGAMI_OK;
 }
@@ -820,6 +896,13 @@ int origami_profile_report(char* buf, uint64_t cap) {
 }
 
 uint64_t origami_launch_count(void) { return g_launches.load(); }
+
+uint32_t origami_get_wait_limit(void) { return wait_limit(); }
+
+int origami_set_wait_limit(uint32_t polls) {
+    g_wait_limit.store(polls, std::memory_order_relaxed);
+    return ORIGAMI_OK;
+}
 
 // ------------------------------------------------------------- tuning --
 int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant) {

@@ -22,7 +22,8 @@ struct LaunchStats;
     uint64_t tile_##name();                                                                               \
     cudaError_t kway_final_##name(const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout, \
                                   void* scratch, cudaStream_t st, int slices,                            \
-                                  void (*on_slice)(void*, uint64_t, uint64_t), void* ctx);
+                                  void (*on_slice)(void*, uint64_t, uint64_t), void* ctx);         \
+    uint64_t kway_final_err_##name(uint64_t n); /* error word's offset in kway_final's scratch */
 ORIGAMI_DECLARE_SORT(u32)
 ORIGAMI_DECLARE_SORT(u64)
 ORIGAMI_DECLARE_SORT(kv)
@@ -56,6 +57,11 @@ SegPlan seg_plan(int kind, uint64_t n, uint64_t nseg);
 void seg_prepare(int kind);
 cudaError_t seg_launch(int kind, void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
                        void* scratch, const SegPlan& p, cudaStream_t st);
+
+// Status of a device error word (bulk.cuh): 1 and 3 mean a bounded bulk-copy
+// wait expired (ORIGAMI_ERR_TIMEOUT), 2 bad segment offsets
+// (ORIGAMI_ERR_INVALID), 0 none.
+inline bool err_word_timeout(int w) { return w == 1 || w == 3; }
 
 // capi.cu: sets the thread's last-error message; makes the stream-ordered pool
 // the caching device arena (returns an ORIGAMI_* status).

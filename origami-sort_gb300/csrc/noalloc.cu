@@ -14,7 +14,7 @@
 // library and stays allocated on each GPU that uses it until the process
 // exits. Its device address is looked up once per device (first call with that
 // device current), so the first call on a device should happen before any
-// stream capture that includes this entry point. Every call shares the one
+// stream capture begins. Every call shares the one
 // array: two calls whose work overlaps on the GPU (different streams, or
 // different host threads) race on it and must be serialized by the caller.
 #include <cstdint>
@@ -81,22 +81,24 @@ extern "C" uint64_t origami_noalloc_max_items(int kind) {
 
 extern "C" int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n,
                                            int flags, void** result, void* stream) {
+    // the size limit first: it holds whatever the buffers are
+    if (origami_noalloc_max_items(kind) > 0 && n > origami_noalloc_max_items(kind))
+        return noalloc_fail(ORIGAMI_ERR_INVALID,
+                            "n exceeds the no-alloc limit (origami_noalloc_max_items)");
     int rc = noalloc_check(kind, d, tmp, n, sort_n, result);
     if (rc != ORIGAMI_OK) return rc;
     if (n > 1 && !tmp) return noalloc_fail(ORIGAMI_ERR_INVALID, "the no-alloc sort needs a tmp buffer");
     if ((((uintptr_t)d) | ((uintptr_t)tmp)) & 15)
         return noalloc_fail(ORIGAMI_ERR_ALIGN, "the no-alloc sort needs 16-byte aligned device buffers");
-    if (n > origami_noalloc_max_items(kind))
-        return noalloc_fail(ORIGAMI_ERR_INVALID,
-                            "n exceeds the no-alloc limit (origami_noalloc_max_items)");
     const bool in_tmp = (flags & ORIGAMI_FLAG_RESULT_IN_TMP) != 0;
+    if (in_tmp && !tmp) return noalloc_fail(ORIGAMI_ERR_INVALID, "RESULT_IN_TMP needs a tmp buffer");
     *result = in_tmp ? tmp : d;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (n <= 1) {
-        if (n == 1 && in_tmp) {
-            cudaError_t e = cudaMemcpyAsync(tmp, d, origami_item_bytes(kind), cudaMemcpyDeviceToDevice, st);
-            if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
-        }
+        cudaError_t e = cudaSuccess;
+        if (n == 1 && in_tmp) e = cudaMemcpyAsync(tmp, d, origami_item_bytes(kind), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess && (flags & ORIGAMI_FLAG_SYNC)) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
         return ORIGAMI_OK;
     }
     int dev = 0;
@@ -118,8 +120,16 @@ extern "C" int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_
     }
     if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
     if (flags & ORIGAMI_FLAG_SYNC) {
-        e = cudaStreamSynchronize(st);
+        // the sort's error word sits right after its splitter slots; the tile
+        // sort cleared it at the start of this call. The copy goes to the
+        // stack (the driver stages it; nothing is allocated).
+        int word = 0;
+        e = cudaMemcpyAsync(&word, reinterpret_cast<const char*>(scratch) + slots_needed(kind, n) * sizeof(int64_t),
+                            sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
+        if (err_word_timeout(word))
+            return noalloc_fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
     }
     return ORIGAMI_OK;
 }

@@ -135,7 +135,7 @@ struct PairMerge {
         if constexpr (BULK) {
             const uint64_t g = tiles < resident() ? tiles : resident();
             launch_dependent(pair_merge_bulk_kernel<T, NT, VT, ST, TILE, MINB>, dim3((unsigned)g), dim3(NT), SMEM, st,
-                             cur, nxt, n, run, splits, tiles, xo, claim, ~0u, err);
+                             cur, nxt, n, run, splits, tiles, xo, claim, ~0u, err, wait_limit());
         } else {
             (void)claim;
             (void)err;
@@ -325,17 +325,19 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                 ahead = wave;
         }
     }
+    // the error word starts at 0: the tile sort clears it, else a memset
+    if (start_run) cudaMemsetAsync(err, 0, sizeof(int), st);
     if (!start_run) {
         T* k1_out = written_by(0);
         launch(n_k1.c_str(), st, [&] {
             if constexpr (C::WARP_K1)
                 warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
                     <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
-                                                                             passes == 0 ? xout : 0, ahead);
+                                                                             passes == 0 ? xout : 0, ahead, err);
             else
                 block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>
                     <<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
-                                                                       passes == 0 ? xout : 0);
+                                                                       passes == 0 ? xout : 0, err);
         });
         if (stats) {
             stats->kernels++;
@@ -392,9 +394,13 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
 // internal order; xout is applied as they are written.
 // `scratch` holds kway_pass_scratch_bytes<T>(n) bytes.
 template <class T>
-uint64_t kway_pass_scratch_bytes(uint64_t n) {
+uint64_t kway_pass_err_offset(uint64_t n) {
     const uint64_t rpg = (n + KwayCfg<T>::RANGE - 1) / KwayCfg<T>::RANGE;
-    return (rpg + 1) * KWAY_MAX * sizeof(int64_t) + 256;
+    return (rpg + 1) * KWAY_MAX * sizeof(int64_t);
+}
+template <class T>
+uint64_t kway_pass_scratch_bytes(uint64_t n) {
+    return kway_pass_err_offset<T>(n) + 256;
 }
 
 template <class T, class OnSlice>
@@ -412,8 +418,9 @@ cudaError_t kway_pass_sliced(const T* in, T* out, uint64_t n, uint64_t run, int 
     if (n == 0) return cudaSuccess;
     const uint64_t rpg = (n + KC::RANGE - 1) / KC::RANGE;
     int64_t* bnd = static_cast<int64_t*>(scratch);
-    int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) + (rpg + 1) * KWAY_MAX * sizeof(int64_t));
+    int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) + kway_pass_err_offset<T>(n));
     const RunLists<T> lists{in, n, run, fan};
+    cudaMemsetAsync(err, 0, sizeof(int), st);
     if (rpg > 1)
         launch(n_ks.c_str(), st, [&] {
             kway_split_kernel<T, RunLists<T>><<<(unsigned)(rpg + 1), 256, 0, st>>>(lists, (int)rpg, 0, bnd, err);

@@ -21,6 +21,11 @@ void count_launches(uint64_t k);
 int prof_begin(const char* name, cudaStream_t st);
 void prof_end(int slot, cudaStream_t st);
 
+// Polls a kernel makes on a bulk-copy barrier before it gives up, reports an
+// expired wait and returns (bulk.cuh). Read when a kernel is launched;
+// origami_set_wait_limit() changes it (default 2^20).
+uint32_t wait_limit();
+
 template <class F>
 inline void launch(const char* name, cudaStream_t st, F&& f) {
     count_launch();

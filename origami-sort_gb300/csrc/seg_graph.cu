@@ -112,7 +112,7 @@ int origami_seg_plan_status(origami_seg_plan* p, void* stream) {
                                     cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return origami::api_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
-    if (herr == 1) return origami::api_fail(ORIGAMI_ERR_TIMEOUT, "a merge job waited past its budget");
+    if (origami::err_word_timeout(herr)) return origami::api_fail(ORIGAMI_ERR_TIMEOUT, "a merge job waited past its budget");
     if (herr == 2) return origami::api_fail(ORIGAMI_ERR_INVALID, "segment offsets decrease");
     return ORIGAMI_OK;
 }

@@ -47,6 +47,7 @@ cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t 
                      void* scratch, int maxl, cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
     SegState s = seg_state<T>(scratch, off, n, nseg, maxl);
+    s.spin = wait_limit();
     const SegGrids<T>& g = seg_grids<T>();
     cudaMemsetAsync(s.err, 0, sizeof(int), st);
     const unsigned b = (unsigned)((nseg + 255) / 256);

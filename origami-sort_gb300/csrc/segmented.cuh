@@ -81,7 +81,8 @@ struct SegState {
     struct SegTileRec* rec;  // geometry of each merge tile of the current level
     unsigned* claim;      // [maxl] tile counter of each level's merge kernel
     uint32_t* tileseg;    // segment of each tile job
-    int* err;             // 2 = bad offsets
+    int* err;             // 1 / 3 = a bulk-copy wait expired (bulk.cuh), 2 = bad offsets
+    uint32_t spin;        // polls before a bulk-copy wait gives up
 };
 
 template <class T>
@@ -195,7 +196,8 @@ struct SegShape {
 //    false when a bulk-copy wait expired (err set).
 template <class T>
 __device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64_t xin, uint64_t xout,
-                              unsigned char* smem, int* split, uint64_t* bar, uint32_t& phase, int* err) {
+                              unsigned char* smem, int* split, uint64_t* bar, uint32_t& phase, int* err,
+                              uint32_t spin) {
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
     constexpr int NT = Sh::NT, NTM = Sh::NTM, VT = C::VT, TILE = C::TILE, WT = 32 * VT;
@@ -209,6 +211,7 @@ __device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
         (void)bar;
         (void)phase;
         (void)err;
+        (void)spin;
 #pragma unroll
         for (int k = 0; k < VT; ++k) {
             const int i = k * NT + tid;
@@ -248,15 +251,12 @@ __device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
             mbar_arrive_expect(bar, (uint32_t)nv * 16u);
             bulk_load(sb, src + (p0 - sh), (uint32_t)nv * 16u, bar);
         }
-        const bool ok = mbar_wait(bar, phase);
-        phase ^= 1u;
+        const bool ok = mbar_wait(bar, phase, spin);
         if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicExch(err, 1);
-                bulk_wait_all();
-            }
+            if (tid == 0) bulk_drain<1>(err, bar, 1u, phase);
             return false;
         }
+        phase ^= 1u;
         if (warp < C::NW && w0 < span) {
             // striped reads: which keys a lane starts with does not matter
             // once the warp's run is sorted
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(SegShape<T>::NTM, SegCfg<T>::TILE_MINB) seg_ti
         const uint64_t p0 = st.off[s] + (uint64_t)t * C::TILE;
         const int cnt = (int)min((uint64_t)C::TILE, g.len - (uint64_t)t * C::TILE);
         if (!seg_tile_sort<T>(d, seg_buf<T>(g.levels, 0, d, tmp), p0, cnt, xmask, g.levels == 0 ? xmask : 0,
-                              smem_raw, split, &bar, phase, st.err))
+                              smem_raw, split, &bar, phase, st.err, st.spin))
             return;
         __syncthreads();
     }
@@ -478,16 +478,14 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
     for (int s = 0;; s ^= 1) {
         const SegBulkGeom q = geom[s];
         if (q.job >= total) break;
-        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
-        phase ^= 1u << s;
+        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u, st.spin);
         if (__syncthreads_or(!ok)) {
-            // no copy into the other stage is in flight yet in this iteration
-            if (tid == 0) {
-                atomicExch(st.err, 1);
-                bulk_wait_all();
-            }
+            // drain this stage's loads (no copy into the other stage is in
+            // flight yet in this iteration)
+            if (tid == 0) bulk_drain<2>(st.err, bar, 1u << s, phase);
             return;
         }
+        phase ^= 1u << s;
         // every thread is past the previous tile's stores from the other
         // stage: thread 0 refills it with the next tile
         if (tid == 0) {
@@ -600,6 +598,7 @@ inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64
     s.err = reinterpret_cast<int*>(take(256));
     s.tileseg = reinterpret_cast<uint32_t*>(take(seg_tile_jobs<T>(n, nseg) * 4));
     s.claim = reinterpret_cast<unsigned*>(take(q * 4));
+    s.spin = BULK_SPIN_LIMIT;
     return s;
 }
 

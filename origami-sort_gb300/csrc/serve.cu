@@ -260,7 +260,7 @@ struct origami_server {
     void retire(Batch& b) {
         const uint64_t ib = item_bytes(b.kind);
         if (b.status == ORIGAMI_OK && b.herr && *b.herr != 0)
-            b.status = *b.herr == 1 ? ORIGAMI_ERR_TIMEOUT : ORIGAMI_ERR_INVALID;
+            b.status = origami::err_word_timeout(*b.herr) ? ORIGAMI_ERR_TIMEOUT : ORIGAMI_ERR_INVALID;
         if (b.status == ORIGAMI_OK) {
             for (size_t i = 0; i < b.reqs.size(); ++i) {
                 const Request& r = *b.reqs[i];

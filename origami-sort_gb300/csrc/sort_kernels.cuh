@@ -31,10 +31,12 @@ struct BlockSortShape {
     static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
 };
 
+// err (optional): the sort's error word, cleared by the first thread (the
+// tile sort is the first kernel of a sort).
 template <class T, int NT, int VTS, int VTM, bool STABLE>
 __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                         uint64_t n, int chunk, uint64_t xin,
-                                                        uint64_t xout) {
+                                                        uint64_t xout, int* err = nullptr) {
     using Sh = BlockSortShape<T, NT, VTS, VTM, STABLE>;
     constexpr int TILE = Sh::TILE;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -42,6 +44,7 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
     T* sb = reinterpret_cast<T*>(smem_raw + Sh::SMEM / 2);
     __shared__ int split[Sh::SPLITS];
     const int tid = threadIdx.x;
+    if (err && blockIdx.x == 0 && tid == 0) *err = 0;
     const uint64_t base = (uint64_t)blockIdx.x * TILE;
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
 
@@ -108,12 +111,14 @@ struct WarpSortShape {
 
 // `ahead` > 0: the CTA first asks for the tile `ahead` places further on to be
 // brought into L2 (the tile a CTA of the next wave will load), so that later
-// CTAs find their keys in L2.
+// CTAs find their keys in L2. err (optional): the sort's error word, cleared by
+// the first thread.
 template <class T, int NW, int VT, int NWT = NW, int MINB = 1>
 __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T* __restrict__ in,
                                                                         T* __restrict__ out, uint64_t n,
                                                                         int chunk, uint64_t xin,
-                                                                        uint64_t xout, uint32_t ahead = 0) {
+                                                                        uint64_t xout, uint32_t ahead = 0,
+                                                                        int* err = nullptr) {
     using Sh = WarpSortShape<T, NW, VT, NWT>;
     static_assert(NWT >= NW, "the sorting warps take part in the merge rounds");
     constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
@@ -127,6 +132,7 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
     static_assert(VT % Vec<T>::N == 0, "lanes load whole vectors");
     const int valid = (int)((n - base) < (uint64_t)TILE ? (n - base) : (uint64_t)TILE);
     const int w0 = warp * WT;
+    if (err && blockIdx.x == 0 && tid == 0) *err = 0;
     if (ahead && tid == 0) {
         const uint64_t pb = base + (uint64_t)ahead * TILE;
         if (pb + TILE <= n) bulk_prefetch_l2(in + pb, (uint32_t)(TILE * sizeof(T)));
@@ -363,7 +369,8 @@ template <class T, int NT, int VT, bool STABLE, int TILE, int MINB = 1>
 __global__ void __launch_bounds__(NT, MINB)
     pair_merge_bulk_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run,
                            const int64_t* __restrict__ splits, uint64_t num_tiles, uint64_t xout,
-                           unsigned* __restrict__ claim, unsigned max_tiles, int* err) {
+                           unsigned* __restrict__ claim, unsigned max_tiles, int* err,
+                           uint32_t spin = BULK_SPIN_LIMIT) {
     using Sh = PairBulkShape<T, NT, VT, STABLE, TILE>;
     constexpr int V = Vec<T>::N;
     constexpr int VO = Block<T, VT, STABLE>::VO;
@@ -425,17 +432,15 @@ __global__ void __launch_bounds__(NT, MINB)
                 ft = claim_next();
             }
         }
-        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
-        phase ^= 1u << s;
+        const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u, spin);
         if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicExch(err, 1);
-                bulk_wait_all();
-                // the other stage's loads, if any, before shared memory goes
-                if (geom[s ^ 1].tile < num_tiles) mbar_wait(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
-            }
+            // drain this stage's loads and the other stage's (if issued)
+            // before shared memory goes
+            if (tid == 0)
+                bulk_drain<2>(err, bar, (1u << s) | (geom[s ^ 1].tile < num_tiles ? 1u << (s ^ 1) : 0u), phase);
             return;
         }
+        phase ^= 1u << s;
         T* buf = stage(s);
         const int total = q.na + q.nb;
         // one merge round, outputs kept in registers until every thread has

@@ -30,6 +30,8 @@ cudaError_t kway_final_u64(const void* in, void* out, uint64_t n, uint64_t run, 
                                 slices, [&](uint64_t o0, uint64_t o1) { on_slice(ctx, o0, o1); });
 }
 
+uint64_t kway_final_err_u64(uint64_t n) { return kway_pass_err_offset<uint64_t>(n); }
+
 uint64_t scratch_bytes_u64(uint64_t n, uint64_t sort_n, int fan) {
     return pipeline_scratch_bytes<uint64_t>(n, sort_n, fan);
 }

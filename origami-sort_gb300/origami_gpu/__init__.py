@@ -86,6 +86,8 @@ def lib():
         L.origami_profile_report.restype = i
         L.origami_profile_report.argtypes = [ctypes.c_char_p, u64]
         L.origami_launch_count.restype = u64
+        L.origami_get_wait_limit.restype = ctypes.c_uint32
+        L.origami_set_wait_limit.argtypes = [ctypes.c_uint32]
         L.origami_sort_segmented_device.restype = i
         L.origami_sort_segmented_device.argtypes = [i, vp, vp, vp, u64, u64, i, vp]
         L.origami_sort_segmented.restype = i
@@ -444,6 +446,17 @@ def profile_report():
 
 def launch_count():
     return int(lib().origami_launch_count())
+
+
+def wait_limit():
+    """Polls a merge kernel makes on a bulk copy before it gives up (default 2^20)."""
+    return int(lib().origami_get_wait_limit())
+
+
+def set_wait_limit(polls):
+    """Sets the device-side wait bound for later launches (0: every first wait
+    expires, which is how the tests drive the expiry path)."""
+    check(lib().origami_set_wait_limit(int(polls)))
 
 
 def empty_host(kind, n, pinned=False):

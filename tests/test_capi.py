@@ -122,3 +122,34 @@ def test_tuning_table_roundtrip(lib, tmp_path):
     og.tuning_set(og.U64, 1 << 24, 2, 0)
     og.tuning_set(og.U32, 1 << 20, 2, 0)
     og.tuning_set(og.KV64, 1 << 27, 2, 0)
+
+
+def test_noalloc_rejects_bad_arguments_on_the_host(lib):
+    # pure host checks, made before the library looks for a device: no buffer
+    # below is ever read or written (they are small host arrays)
+    a = np.zeros(64, np.uint32)
+    b = np.zeros(64, np.uint32)
+    res = ctypes.c_void_p()
+    limit = lib.origami_noalloc_max_items(og.U32)
+    assert limit >= (1 << 28)  # the 1 GiB uint32 workload fits
+    assert lib.origami_noalloc_max_items(og.KV64) >= (1 << 26)
+    assert lib.origami_noalloc_max_items(9) == 0
+    rc = lib.origami_sort_noalloc_device(og.U32, a.ctypes.data, b.ctypes.data, limit + 1, 0, 0,
+                                         ctypes.byref(res), None)
+    assert rc == og.ERR_INVALID
+    assert b"limit" in lib.origami_last_error()
+    # a tmp buffer is required, RESULT_IN_TMP too, even for one item
+    assert lib.origami_sort_noalloc_device(og.U32, a.ctypes.data, None, 64, 0, 0, ctypes.byref(res),
+                                           None) == og.ERR_INVALID
+    assert lib.origami_sort_noalloc_device(og.U32, a.ctypes.data, None, 1, 0, og.FLAG_RESULT_IN_TMP,
+                                           ctypes.byref(res), None) == og.ERR_INVALID
+    assert lib.origami_sort_noalloc_device(9, a.ctypes.data, b.ctypes.data, 64, 0, 0, ctypes.byref(res),
+                                           None) == og.ERR_DTYPE
+
+
+def test_wait_limit_is_host_state(lib):
+    default = lib.origami_get_wait_limit()
+    assert default == 1 << 20
+    assert lib.origami_set_wait_limit(77) == og.OK
+    assert lib.origami_get_wait_limit() == 77
+    assert lib.origami_set_wait_limit(default) == og.OK

@@ -1,4 +1,6 @@
-"""GPU parity tests of the batched segmented sort (one persistent launch).
+"""GPU parity tests of the batched segmented sort (a device-planned tile phase,
+then one partition and one persistent merge kernel per merge level over all
+segments at once; the plan form replays that sequence as a CUDA graph).
 
 Every segment must equal an independent stable sort of that segment: numpy for
 key-value items; for keys-only items also the oracle, which restates the

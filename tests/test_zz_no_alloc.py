@@ -7,6 +7,9 @@ library's device image instead of arena memory. These tests call it through
 the C ABI, twice in a row on the same device (the array keeps the previous
 call's contents), and require the same bytes as the regular device entry
 point, exactly: the sort is integer work, so the tolerance is zero.
+
+The size limit and the argument checks are host logic and are tested on the
+CPU (tests/test_capi.py), with buffers that are never touched.
 """
 import ctypes
 
@@ -32,29 +35,31 @@ def _random_bytes(n_items, kind, seed):
     return torch.randint(0, 256, (nbytes,), dtype=torch.uint8, device="cuda", generator=g)
 
 
-def _regular(kind, src, n, sort_n):
+def _regular(kind, src, n, sort_n, flags=0):
     d = src.clone()
     t = torch.empty_like(d)
     res = ctypes.c_void_p()
     s = torch.cuda.current_stream().cuda_stream
-    og.check(og.lib().origami_sort_device(kind, d.data_ptr(), t.data_ptr(), n, sort_n, 2, 0,
+    og.check(og.lib().origami_sort_device(kind, d.data_ptr(), t.data_ptr(), n, sort_n, 2, flags,
                                           ctypes.byref(res), ctypes.c_void_p(s)))
     torch.cuda.synchronize()
-    return (d if res.value == d.data_ptr() else t).cpu().numpy()
+    return d if res.value == d.data_ptr() else t
 
 
-def _noalloc(kind, src, n, sort_n):
+def _noalloc(kind, src, n, sort_n, flags=0):
     d = src.clone()
     t = torch.empty_like(d)
     res = ctypes.c_void_p()
     s = torch.cuda.current_stream().cuda_stream
-    og.check(og.lib().origami_sort_noalloc_device(kind, d.data_ptr(), t.data_ptr(), n, sort_n, 0,
+    og.check(og.lib().origami_sort_noalloc_device(kind, d.data_ptr(), t.data_ptr(), n, sort_n, flags,
                                                   ctypes.byref(res), ctypes.c_void_p(s)))
     torch.cuda.synchronize()
-    return (d if res.value == d.data_ptr() else t).cpu().numpy()
+    want = t if flags & og.FLAG_RESULT_IN_TMP else d
+    assert res.value == want.data_ptr()
+    return want
 
 
-@pytest.mark.parametrize("kind", [og.U32, og.I64, og.KV64])
+@pytest.mark.parametrize("kind", [og.U32, og.U64, og.I64, og.KV64, og.KVU64])
 @pytest.mark.parametrize("sort_n", [0, 1 << 16])
 def test_noalloc_matches_regular_entry_point_twice(kind, sort_n):
     n = 3 * (1 << 20) + 77
@@ -62,17 +67,37 @@ def test_noalloc_matches_regular_entry_point_twice(kind, sort_n):
         src = _random_bytes(n, kind, seed + kind)
         expect = _regular(kind, src, n, sort_n)
         got = _noalloc(kind, src, n, sort_n)
-        assert np.array_equal(got, expect), f"call {call}"
+        assert torch.equal(got, expect), f"call {call}"
 
 
-def test_noalloc_rejects_sizes_beyond_its_limit():
-    kind = og.U32
-    limit = og.lib().origami_noalloc_max_items(kind)
-    assert limit >= (1 << 28)  # the 1 GiB workload fits
-    buf = torch.empty(64, dtype=torch.uint8, device="cuda")
-    res = ctypes.c_void_p()
-    far = buf.data_ptr() + (1 << 44)  # never dereferenced: the call is rejected first
-    rc = og.lib().origami_sort_noalloc_device(kind, buf.data_ptr(), far, limit + 1, 0, 0,
-                                              ctypes.byref(res), None)
-    assert rc == og.ERR_INVALID
-    assert b"limit" in og.lib().origami_last_error()
+@pytest.mark.parametrize("flags", [og.FLAG_RESULT_IN_TMP, og.FLAG_RESULT_IN_TMP | og.FLAG_SYNC, og.FLAG_SYNC])
+@pytest.mark.parametrize("kind", [og.U32, og.KV64])
+def test_noalloc_result_buffer_and_sync(kind, flags):
+    n = (1 << 18) + 5
+    for seed in (11, 12):
+        src = _random_bytes(n, kind, seed)
+        expect = _regular(kind, src, n, 0, flags & og.FLAG_RESULT_IN_TMP)
+        got = _noalloc(kind, src, n, 0, flags)
+        assert torch.equal(got, expect)
+
+
+@pytest.mark.parametrize("flags", [0, og.FLAG_RESULT_IN_TMP, og.FLAG_RESULT_IN_TMP | og.FLAG_SYNC])
+def test_noalloc_zero_and_one_item(flags):
+    for n in (0, 1):
+        src = _random_bytes(max(n, 1), og.KV64, 5)
+        got = _noalloc(og.KV64, src, n, 0, flags)
+        if n == 1:
+            assert torch.equal(got, src)
+
+
+def test_noalloc_at_the_headline_size_twice():
+    # 268,435,456 uint32 keys (1 GiB): the far end of the scratch array is used
+    n = 1 << 28
+    assert n <= og.lib().origami_noalloc_max_items(og.U32)
+    for seed in (31, 32):
+        src = _random_bytes(n, og.U32, seed)
+        expect = _regular(og.U32, src, n, 0)
+        got = _noalloc(og.U32, src, n, 0, og.FLAG_SYNC)
+        assert torch.equal(got, expect)
+        del expect, got, src
+        torch.cuda.empty_cache()
