@@ -10,8 +10,13 @@
 //
 // Error words written by the kernels (int, 0 = no error):
 //   1  a bulk-copy wait expired; the copies it waited for were drained
+//   2  (segmented sort) decreasing or out-of-range segment offsets
 //   3  a bulk-copy wait expired and a drain wait expired too: copies may still
 //      have been in flight when the CTA returned
+//   5  merge splits that are inconsistent: the runs given to a merge were not
+//      sorted (the tile was clamped so that every access stays in bounds)
+// A merge kernel that finds 1 or 3 already set returns at once: the passes
+// after an expired wait would merge runs that are not sorted.
 #pragma once
 #include <cstdint>
 
@@ -20,6 +25,14 @@ namespace origami {
 constexpr uint32_t BULK_SPIN_LIMIT = 1u << 20;
 constexpr int ERR_WAIT_EXPIRED = 1;
 constexpr int ERR_WAIT_UNDRAINED = 3;
+constexpr int ERR_BAD_RUNS = 5;
+
+__device__ __forceinline__ bool err_wait_set(const int* err) {
+    const int w = *(volatile const int*)err;
+    return w == ERR_WAIT_EXPIRED || w == ERR_WAIT_UNDRAINED;
+}
+// Records a first error (an earlier one is kept).
+__device__ __forceinline__ void err_first(int* err, int code) { atomicCAS(err, 0, code); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -101,13 +114,14 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 // If one of those waits expires as well, records ERR_WAIT_UNDRAINED.
 template <int NB>
 __device__ __forceinline__ void bulk_drain(int* err, uint64_t* bars, uint32_t pending, uint32_t parity) {
-    atomicMax(err, ERR_WAIT_EXPIRED);
+    atomicCAS(err, 0, ERR_WAIT_EXPIRED);
+    atomicCAS(err, ERR_BAD_RUNS, ERR_WAIT_EXPIRED);
     bulk_wait_all();
     bool drained = true;
 #pragma unroll
     for (int i = 0; i < NB; ++i)
         if ((pending >> i) & 1u) drained = mbar_wait(&bars[i], (parity >> i) & 1u) && drained;
-    if (!drained) atomicMax(err, ERR_WAIT_UNDRAINED);
+    if (!drained) atomicExch(err, ERR_WAIT_UNDRAINED);
 }
 
 // Programmatic dependent launch. A kernel launched with the programmatic

@@ -19,6 +19,7 @@
 // Ties: items are ordered by (key, run index, position), which makes the merge
 // stable across runs and gives every item exactly one place.
 #pragma once
+#include "bulk.cuh"
 #include "common.cuh"
 #include "merge_core.cuh"
 
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(256) kway_split_kernel(const Lists lists, int 
             hi[tid] = (int64_t)nhi[tid];
         }
         __syncthreads();
-        if (round == 79 && tid == 0) atomicExch(err, 1);  // cannot happen: windows halve
+        if (round == 79 && tid == 0) err_first(err, ERR_BAD_RUNS);  // sorted runs: windows halve, never 80 rounds
     }
     if (tid < KWAY_MAX) out[tid] = lo[tid];
 }
@@ -274,10 +275,14 @@ struct NoProbe {
 // caller's buffer); xout: flip applied as they are written.
 // block0 offsets the block index, so that a pass can be launched in slices of
 // consecutive ranges.
+// Runs that are not sorted (the caller's streams) can give inconsistent
+// bounds and cuts: every range and tile is then clamped into its runs and the
+// shared-memory capacities, err (optional) receives ERR_BAD_RUNS, and nothing
+// is read or written out of bounds.
 template <class T, class Lists, class C = KwayCfg<T>, class Probe = NoProbe>
 __global__ void __launch_bounds__(C::NT) range_merge_kernel(
     const Lists lists, T* __restrict__ dst, int rpg, const int64_t* __restrict__ bnd, uint64_t xin,
-    uint64_t xout, uint32_t block0 = 0, Probe probe = Probe()) {
+    uint64_t xout, uint32_t block0 = 0, Probe probe = Probe(), int* err = nullptr) {
     static_assert(C::STABLE || !Traits<T>::kStable, "key-value items need the stable merge");
     using Lay = KwayLayout<T, C>;
     using K = typename Traits<T>::Key;
@@ -310,6 +315,12 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
             a = bb[tid];
             e = bb[KWAY_MAX + tid];
         }
+        // bounds of sorted runs always hold this
+        if (a < 0 || a > (int64_t)L || e < a || e > (int64_t)L) {
+            if (err) err_first(err, ERR_BAD_RUNS);
+            a = a < 0 ? 0 : (a > (int64_t)L ? (int64_t)L : a);
+            e = e < a ? a : (e > (int64_t)L ? (int64_t)L : e);
+        }
         lo[tid] = geo.list(tid) + a;
         skip[tid] = a;
         len[tid] = (uint32_t)(e - a);
@@ -325,6 +336,14 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
             o += (int)(len[q] / S);
         }
         off[KWAY_MAX] = o;
+        if (o > Lay::SCAP) {  // a range of sorted runs never holds more samples
+            if (err) err_first(err, ERR_BAD_RUNS);
+            for (int q = 0; q < KWAY_MAX; ++q) {
+                off[q] = 0;
+                len[q] = 0;
+            }
+            off[KWAY_MAX] = 0;
+        }
     }
     __syncthreads();
     const int nsamp = off[KWAY_MAX];
@@ -402,7 +421,19 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
         sp[q] = v;
     }
     __syncthreads();
-    // per-tile list offsets: toff[t][q] = items of tile t taken from runs < q
+    // cuts of sorted runs only move forward; make sure of it
+    if (tid < KWAY_MAX) {
+        for (int b = 1; b <= nt; ++b) {
+            uint32_t& v = sp[b * KWAY_MAX + tid];
+            if (v < sp[(b - 1) * KWAY_MAX + tid]) {
+                v = sp[(b - 1) * KWAY_MAX + tid];
+                if (err) err_first(err, ERR_BAD_RUNS);
+            }
+        }
+    }
+    __syncthreads();
+    // per-tile list offsets: toff[t][q] = items of tile t taken from runs < q;
+    // a tile larger than the buffers (runs that are not sorted) is left out
     for (int t = tid; t < nt; t += NT) {
         int o = 0;
         for (int q = 0; q < KWAY_MAX; ++q) {
@@ -410,6 +441,10 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
             o += (int)(sp[(t + 1) * KWAY_MAX + q] - sp[t * KWAY_MAX + q]);
         }
         toff[t * (KWAY_MAX + 1) + KWAY_MAX] = o;
+        if (o > C::TMAX) {
+            if (err) err_first(err, ERR_BAD_RUNS);
+            for (int q = 0; q <= KWAY_MAX; ++q) toff[t * (KWAY_MAX + 1) + q] = 0;
+        }
     }
     __syncthreads();
 
@@ -419,7 +454,7 @@ __global__ void __launch_bounds__(C::NT) range_merge_kernel(
         const int* to = toff + t * (KWAY_MAX + 1);
         for (int q = 0; q < geo.nr; ++q) {
             const int o0 = to[q];
-            const int l = to[q + 1] - o0;
+            const int l = (to[KWAY_MAX] == 0) ? 0 : to[q + 1] - o0;
             const T* rp = lo[q] + sp[t * KWAY_MAX + q];
             for (int k = tid; k < l; k += NT) cp_async_item(&b[o0 + k], rp + k);
         }

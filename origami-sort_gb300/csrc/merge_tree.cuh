@@ -144,7 +144,7 @@ struct MergeTreeOps {
         }
         launch(n_km.c_str(), st, [&] {
             range_merge_kernel<T, StreamLists<T>><<<(unsigned)rpg, C::NT, KwayLayout<T>::SMEM, st>>>(
-                sl, dst, (int)rpg, bnd, xin, xout);
+                sl, dst, (int)rpg, bnd, xin, xout, 0, NoProbe(), err);
         });
         if (bnd) cudaFreeAsync(bnd, st);
         return cudaGetLastError();

@@ -6,6 +6,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <utility>
@@ -138,8 +139,8 @@ struct PairMerge {
                              cur, nxt, n, run, splits, tiles, xo, claim, ~0u, err, wait_limit());
         } else {
             (void)claim;
-            (void)err;
-            pair_merge_kernel<T, NT, VT, ST, TILE, MINB><<<(unsigned)tiles, NT, SMEM, st>>>(cur, nxt, n, run, splits, xo);
+            pair_merge_kernel<T, NT, VT, ST, TILE, MINB><<<(unsigned)tiles, NT, SMEM, st>>>(cur, nxt, n, run, splits, xo,
+                                                                                           err);
         }
     }
 };
@@ -153,6 +154,20 @@ using PairMerge2 =
 // overlap another's merges (a persistent kernel holds the SMs until it drains).
 template <class T>
 using PairMergeI = PairMerge<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::P_TILE, Config<T>::PI_MINB, false>;
+
+// Resident CTAs of the k-way merge kernel on the whole GPU (its persistent grid).
+template <class T>
+uint64_t kb_resident() {
+    static const uint64_t r = [] {
+        cudaFuncSetAttribute(kb_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KbShape<T>::SMEM);
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_merge_kernel<T>, KbCfg<T>::NT, KbShape<T>::SMEM);
+        return (uint64_t)sms * (uint64_t)(per > 0 ? per : 1);
+    }();
+    return r;
+}
 
 static_assert(Config<uint32_t>::P2_TILE >= Config<uint32_t>::P_TILE && Config<uint64_t>::P2_TILE >= Config<uint64_t>::P_TILE &&
                   Config<KV64>::P2_TILE >= Config<KV64>::P_TILE,
@@ -212,8 +227,7 @@ std::vector<PassPlan> plan_passes(uint64_t n, uint64_t limit, int fan, uint64_t 
             if (p.fan < 2) p.fan = 2;
             const uint64_t G = run * (uint64_t)p.fan;
             p.groups = (n + G - 1) / G;
-            const uint64_t R = KwayCfg<T>::RANGE;
-            p.rpg = G <= R ? 1 : (int)((G + R - 1) / R);
+            p.rpg = kb_ranges_per_group<T>(run, p.fan);
         }
         v.push_back(p);
         run *= (uint64_t)p.fan;
@@ -225,19 +239,65 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
     return (sort_n == 0 || sort_n >= n) ? n : sort_n;
 }
 
-// Device scratch (bytes) one sort needs: binary splits or k-way range bounds,
-// plus an error word and the merge kernel's tile counter (256 bytes).
+// Device scratch of one sort, in this order (each part 256-byte aligned):
+//   splits     binary passes: one int64 per merge tile + 2
+//   k-way passes (only when the plan has some, kway_bulk.cuh):
+//   bnd0       super-sample splits of the range boundaries, [groups][rpg+1][16]
+//   tab        tile cuts, [ranges][TPR+1][16] int64
+//   ntiles     tiles per range
+//   samp 0/1   samples (one key per S items) of the runs a pass reads / writes
+//   ssamp 0/1  super-samples (one key per S*64 items)
+//   tail       256 bytes: the error word, then the merge kernels' tile counter
+template <class T>
+struct PipeScratch {
+    using K = typename Traits<T>::Key;
+    uint64_t bytes = 0;  // total, tail included
+    int64_t* splits = nullptr;
+    int64_t* bnd0 = nullptr;
+    int64_t* tab = nullptr;
+    uint32_t* ntiles = nullptr;
+    K* samp[2] = {nullptr, nullptr};
+    K* ssamp[2] = {nullptr, nullptr};
+    int* err = nullptr;
+    unsigned* claim = nullptr;
+    PipeScratch(void* base, uint64_t n, uint64_t sort_n, int code, uint64_t start_run) {
+        char* b = static_cast<char*>(base);
+        uint64_t o = 0;
+        auto take = [&](uint64_t sz) {
+            char* r = b ? b + o : nullptr;
+            o += (sz + 255) & ~255ull;
+            return r;
+        };
+        uint64_t bnd_b = 0, tab_b = 0, rng = 0;
+        bool kway = false;
+        for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), shape_fan(code), start_run)) {
+            if (p.fan <= 2) continue;
+            kway = true;
+            const uint64_t r = p.groups * (uint64_t)p.rpg;
+            if (p.rpg > 1) bnd_b = std::max<uint64_t>(bnd_b, p.groups * (uint64_t)(p.rpg + 1) * KWAY_MAX * 8);
+            tab_b = std::max<uint64_t>(tab_b, r * (uint64_t)(KbShape<T>::TPR + 1) * KWAY_MAX * 8);
+            rng = std::max<uint64_t>(rng, r);
+        }
+        splits = reinterpret_cast<int64_t*>(take(merge_split_slots<T>(n) * sizeof(int64_t)));
+        if (kway) {
+            constexpr uint64_t S = KbCfg<T>::S;
+            if (bnd_b) bnd0 = reinterpret_cast<int64_t*>(take(bnd_b));
+            tab = reinterpret_cast<int64_t*>(take(tab_b));
+            ntiles = reinterpret_cast<uint32_t*>(take(rng * 4));
+            for (int i = 0; i < 2; ++i) samp[i] = reinterpret_cast<K*>(take((n / S + 1) * sizeof(K)));
+            for (int i = 0; i < 2; ++i) ssamp[i] = reinterpret_cast<K*>(take((n / (S * KB_SS) + 1) * sizeof(K)));
+        }
+        err = reinterpret_cast<int*>(take(256));
+        claim = b ? reinterpret_cast<unsigned*>(reinterpret_cast<char*>(err) + 64) : nullptr;
+        bytes = o;
+    }
+};
+
+// Device scratch (bytes) one sort needs (PipeScratch); the error word is the
+// first int of its last 256 bytes.
 template <class T>
 uint64_t pipeline_scratch_bytes(uint64_t n, uint64_t sort_n, int code, uint64_t start_run = 0) {
-    const int fan = shape_fan(code);
-    uint64_t bytes = merge_split_slots<T>(n) * sizeof(int64_t);
-    for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), fan, start_run)) {
-        if (p.fan > 2 && p.rpg > 1) {
-            const uint64_t b = p.groups * (uint64_t)(p.rpg + 1) * KWAY_MAX * sizeof(int64_t);
-            bytes = b > bytes ? b : bytes;
-        }
-    }
-    return bytes + 256;
+    return PipeScratch<T>(nullptr, n, sort_n, code, start_run).bytes;
 }
 
 // Sorts in[0..n) in chunks of sort_n (0 = one full sort) into out[0..n).
@@ -276,10 +336,16 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     // last, then wa, wb, wa, ... going backwards
     auto written_by = [&](int k) -> T* { return k == passes ? out : (((passes - k) & 1) ? wa : wb); };
     const T* cur = start_run ? in : written_by(0);
-    int64_t* splits = static_cast<int64_t*>(scratch);
-    int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) +
-                                      pipeline_scratch_bytes<T>(n, sort_n, code, start_run) - 256);
-    unsigned* claim = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(err) + 64);
+    const PipeScratch<T> sc(scratch, n, sort_n, code, start_run);
+    int64_t* splits = sc.splits;
+    int* err = sc.err;
+    unsigned* claim = sc.claim;
+    using K = typename Traits<T>::Key;
+    // samples for the first k-way pass: written by the tile sort, or gathered
+    // from runs the caller gave (start_run)
+    const bool kw_first = passes > 0 && plan[0].fan > 2;
+    K* k1_samp = (kw_first && !start_run) ? sc.samp[0] : nullptr;
+    K* k1_ssamp = (kw_first && !start_run) ? sc.ssamp[0] : nullptr;
 
     // kernel attributes, once per process (thread-safe static initialisation)
     static const bool configured = [] {
@@ -294,6 +360,9 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         PairMergeI<T>::configure();
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
+        cudaFuncSetAttribute(kb_cut_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)KbShape<T>::CUT_SMEM);
+        cudaFuncSetAttribute(kb_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KbShape<T>::SMEM);
         return true;
     }();
     (void)configured;
@@ -302,7 +371,9 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     static const std::string n_k4 = std::string("pair_partition<") + TypeName<T>::v + ">";
     static const std::string n_k3 = std::string("pair_merge<") + TypeName<T>::v + ">";
     static const std::string n_ks = std::string("kway_split<") + TypeName<T>::v + ">";
+    static const std::string n_kc = std::string("kway_cut<") + TypeName<T>::v + ">";
     static const std::string n_km = std::string("kway_merge<") + TypeName<T>::v + ">";
+    static const std::string n_kg = std::string("kway_samples<") + TypeName<T>::v + ">";
     const uint64_t tiles1 = (n + T1 - 1) / T1;
     // the tile sort prefetches into L2 the tile one wave of resident CTAs
     // further on (input in device memory only; 1 GiB: 1.89 -> 1.82 ms)
@@ -332,12 +403,13 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         launch(n_k1.c_str(), st, [&] {
             if constexpr (C::WARP_K1)
                 warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
-                    <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
-                                                                             passes == 0 ? xout : 0, ahead, err);
+                    <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
+                        in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err, k1_samp, k1_ssamp);
             else
                 block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>
                     <<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
-                                                                       passes == 0 ? xout : 0, err);
+                                                                       passes == 0 ? xout : 0, err, k1_samp,
+                                                                       k1_ssamp);
         });
         if (stats) {
             stats->kernels++;
@@ -367,18 +439,40 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
             });
             if (stats) stats->kernels += 2;
         } else {
+            // sampled k-way pass (kway_bulk.cuh): samples of `cur` are in set
+            // pi & 1; the pass writes set (pi+1) & 1 when a k-way pass follows
+            constexpr uint64_t S = KbCfg<T>::S, SS = KB_SS;
+            K* s_in = sc.samp[pi & 1];
+            K* ss_in = sc.ssamp[pi & 1];
+            const bool more = pi + 1 < passes && plan[pi + 1].fan > 2;
+            K* s_out = more ? sc.samp[(pi + 1) & 1] : nullptr;
+            K* ss_out = more ? sc.ssamp[(pi + 1) & 1] : nullptr;
+            if (pi == 0 && start_run) {
+                const uint64_t ns = n / S;
+                const unsigned gb = (unsigned)std::min<uint64_t>((ns + 255) / 256 + 1, 152ull * 16);
+                launch(n_kg.c_str(), st, [&] { kb_gather_samples_kernel<T><<<gb, 256, 0, st>>>(cur, n, s_in, ss_in); });
+                if (stats) stats->kernels++;
+            }
             if (p.rpg > 1) {
                 launch(n_ks.c_str(), st, [&] {
-                    kway_split_kernel<T, RunLists<T>><<<(unsigned)(p.groups * (p.rpg + 1)), 256, 0, st>>>(
-                        RunLists<T>{cur, n, p.run, p.fan}, p.rpg, 0, splits, err);
+                    kway_split_kernel<K, RunLists<K>><<<(unsigned)(p.groups * (p.rpg + 1)), 256, 0, st>>>(
+                        RunLists<K>{ss_in, n / (S * SS), p.run / (S * SS), p.fan}, p.rpg, 0, sc.bnd0, err);
                 });
                 if (stats) stats->kernels++;
             }
-            launch(n_km.c_str(), st, [&] {
-                range_merge_kernel<T, RunLists<T>><<<(unsigned)(p.groups * p.rpg), KC::NT, KwayLayout<T>::SMEM, st>>>(
-                    RunLists<T>{cur, n, p.run, p.fan}, nxt, p.rpg, p.rpg > 1 ? splits : nullptr, 0, xo);
+            const uint64_t ranges = p.groups * (uint64_t)p.rpg;
+            launch(n_kc.c_str(), st, [&] {
+                kb_cut_kernel<T><<<(unsigned)ranges, KB_CUT_NT, KbShape<T>::CUT_SMEM, st>>>(
+                    cur, s_in, n, p.run, p.fan, p.rpg, sc.bnd0, sc.tab, sc.ntiles, claim, err);
             });
-            if (stats) stats->kernels++;
+            const uint64_t nslots = ranges * (uint64_t)KbShape<T>::TPR;
+            const uint64_t grid = std::min<uint64_t>(nslots, kb_resident<T>());
+            launch(n_km.c_str(), st, [&] {
+                kb_merge_kernel<T><<<(unsigned)grid, KbCfg<T>::NT, KbShape<T>::SMEM, st>>>(
+                    cur, nxt, n, p.run, p.fan, p.rpg, sc.tab, sc.ntiles, nslots, xo, s_out, ss_out, claim, err,
+                    wait_limit());
+            });
+            if (stats) stats->kernels += 2;
         }
         if (stats) stats->passes++;
         cur = nxt;
@@ -431,7 +525,7 @@ cudaError_t kway_pass_sliced(const T* in, T* out, uint64_t n, uint64_t run, int 
         const uint64_t b0 = rpg * sl / slices, b1 = rpg * (sl + 1) / slices;
         launch(n_km.c_str(), st, [&] {
             range_merge_kernel<T, RunLists<T>><<<(unsigned)(b1 - b0), KC::NT, KwayLayout<T>::SMEM, st>>>(
-                lists, out, (int)rpg, rpg > 1 ? bnd : nullptr, 0, xout, (uint32_t)b0);
+                lists, out, (int)rpg, rpg > 1 ? bnd : nullptr, 0, xout, (uint32_t)b0, NoProbe(), err);
         });
         // range b starts at output b * n / rpg (kway_split_kernel's boundaries)
         on_slice((uint64_t)(((unsigned __int128)b0 * n) / rpg), (uint64_t)(((unsigned __int128)b1 * n) / rpg));

@@ -360,7 +360,7 @@ struct SegPair {
 // kernel: the pair's first item, the tile's output range within the pair, the
 // A run length and four flags in its top bits.
 struct SegTileRec {
-    uint64_t base, d0, d1, la_flags;
+    uint64_t base, d0, d1, la_flags, lb;
     static constexpr uint64_t SRC_TMP = 1ull << 60, DST_TMP = 1ull << 61, LAST = 1ull << 62, PAIR_END = 1ull << 63;
     static constexpr uint64_t LA_MASK = (1ull << 60) - 1;
 };
@@ -391,6 +391,7 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
         r.d0 = p.d0;
         r.d1 = p.d1;
         r.la_flags = f;
+        r.lb = p.lb;
         st.rec[j] = r;
     }
 }
@@ -408,16 +409,21 @@ struct SegBulkGeom {
     uint64_t flags;
 };
 
+// Splits that are inconsistent (runs that are not sorted) are clamped into
+// the runs and reported in *err (ERR_BAD_RUNS).
 template <class T>
 __device__ __forceinline__ SegBulkGeom seg_bulk_issue(T* stage, const T* d, const T* tmp, uint64_t j,
-                                                      const SegTileRec& r, int64_t s0, int64_t s1, uint64_t* bar) {
+                                                      const SegTileRec& r, int64_t s0, int64_t s1, uint64_t* bar,
+                                                      int* err) {
     constexpr int V = Vec<T>::N;
     const uint64_t la = r.la_flags & SegTileRec::LA_MASK;
     const int64_t a1 = (r.la_flags & SegTileRec::PAIR_END) ? (int64_t)la : s1;
     SegBulkGeom q;
     q.job = j;
     q.flags = r.la_flags;
-    q.na = (int)(a1 - s0);
+    bool bad = false;
+    q.na = (int)tile_split(s0, a1, (int64_t)r.d0, (int64_t)(r.d1 - r.d0), (int64_t)la, (int64_t)r.lb, &bad);
+    if (bad) err_first(err, ERR_BAD_RUNS);
     q.nb = (int)(r.d1 - r.d0) - q.na;
     q.obase = r.base + r.d0;
     q.sh = (int)(q.obase % V);
@@ -452,6 +458,8 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
     const uint64_t total = st.tot[1 + l];
     const uint64_t G = gridDim.x;
     if (blockIdx.x >= total) return;
+    // a wait of an earlier kernel expired: the runs are not sorted, stop here
+    if (__syncthreads_or(tid == 0 && err_wait_set(st.err))) return;
     unsigned* claim = st.claim + l;
     auto stage = [&](int s) { return reinterpret_cast<T*>(smem_raw + (size_t)s * Sh::STAGE); };
     auto claim_next = [&] { return G + (uint64_t)atomicAdd(claim, 1u); };
@@ -464,7 +472,8 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         mbar_init(&bar[1], 1);
         mbar_init_fence();
         const uint64_t j0 = blockIdx.x;
-        geom[0] = seg_bulk_issue<T>(stage(0), d, tmp, j0, st.rec[j0], st.splits[j0], st.splits[j0 + 1], &bar[0]);
+        geom[0] = seg_bulk_issue<T>(stage(0), d, tmp, j0, st.rec[j0], st.splits[j0], st.splits[j0 + 1], &bar[0],
+                                    st.err);
         nj = claim_next();
         if (nj < total) {
             nr = st.rec[nj];
@@ -491,7 +500,7 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         if (tid == 0) {
             if (nj < total) {
                 bulk_wait_read<0>();
-                geom[s ^ 1] = seg_bulk_issue<T>(stage(s ^ 1), d, tmp, nj, nr, n0, n1, &bar[s ^ 1]);
+                geom[s ^ 1] = seg_bulk_issue<T>(stage(s ^ 1), d, tmp, nj, nr, n0, n1, &bar[s ^ 1], st.err);
             } else {
                 geom[s ^ 1].job = total;
             }

@@ -9,6 +9,7 @@
 #pragma once
 #include "bulk.cuh"
 #include "common.cuh"
+#include "kway_bulk.cuh"
 #include "merge_core.cuh"
 #include "warp_sort.cuh"
 
@@ -32,11 +33,14 @@ struct BlockSortShape {
 };
 
 // err (optional): the sort's error word, cleared by the first thread (the
-// tile sort is the first kernel of a sort).
+// tile sort is the first kernel of a sort). samp / ssamp (optional): samples
+// of the sorted tiles for a k-way pass that follows (kway_bulk.cuh).
 template <class T, int NT, int VTS, int VTM, bool STABLE>
 __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in, T* __restrict__ out,
                                                         uint64_t n, int chunk, uint64_t xin,
-                                                        uint64_t xout, int* err = nullptr) {
+                                                        uint64_t xout, int* err = nullptr,
+                                                        typename Traits<T>::Key* samp = nullptr,
+                                                        typename Traits<T>::Key* ssamp = nullptr) {
     using Sh = BlockSortShape<T, NT, VTS, VTM, STABLE>;
     constexpr int TILE = Sh::TILE;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -83,6 +87,7 @@ __global__ void __launch_bounds__(NT) block_sort_kernel(const T* __restrict__ in
             const int i = k * NT + tid;
             if (i < valid) out[base + i] = Traits<T>::flip(src[i], xout);
         }
+        if (samp) kb_emit_samples<T>(src, base, valid, samp, ssamp, NT);
     } else {
 #pragma unroll
         for (int k = 0; k < VTS; ++k) {
@@ -118,7 +123,9 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
                                                                         T* __restrict__ out, uint64_t n,
                                                                         int chunk, uint64_t xin,
                                                                         uint64_t xout, uint32_t ahead = 0,
-                                                                        int* err = nullptr) {
+                                                                        int* err = nullptr,
+                                                                        typename Traits<T>::Key* samp = nullptr,
+                                                                        typename Traits<T>::Key* ssamp = nullptr) {
     using Sh = WarpSortShape<T, NW, VT, NWT>;
     static_assert(NWT >= NW, "the sorting warps take part in the merge rounds");
     constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
@@ -191,6 +198,7 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
             *reinterpret_cast<uint4*>(out + base + (size_t)i * V) = *reinterpret_cast<const uint4*>(e);
         }
         for (int i = nvec * V + tid; i < valid; i += Sh::NTM) out[base + i] = Traits<T>::flip(src[i], xout);
+        if (samp) kb_emit_samples<T>(src, base, valid, samp, ssamp, Sh::NTM);
     } else if (sorter) {
         // runs end at the warp (or chunk) size: each lane stores its own keys
         const int i0 = w0 + lane * VT;
@@ -271,7 +279,7 @@ template <class T, int NT, int VT, bool STABLE, int TILE, int MINB = 1>
 __global__ void __launch_bounds__(NT, MINB) pair_merge_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                         uint64_t n, uint64_t run,
                                                         const int64_t* __restrict__ splits,
-                                                        uint64_t xout) {
+                                                        uint64_t xout, int* err) {
     using Sh = PairShape<T, NT, VT, STABLE, TILE>;
     constexpr int V = Sh::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -284,10 +292,13 @@ __global__ void __launch_bounds__(NT, MINB) pair_merge_kernel(const T* __restric
     const uint64_t d0 = o - g.pbase;
     const uint64_t pair_end = g.la + g.lb;
     const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
-    const int64_t a0 = splits[t];
+    if (__syncthreads_or(tid == 0 && err_wait_set(err))) return;  // an earlier pass gave up
+    int64_t a0 = splits[t];
     const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
-    const int na = (int)(a1 - a0);
     const int total = (int)(d1 - d0);
+    bool bad = false;
+    const int na = (int)tile_split(a0, a1, (int64_t)d0, (int64_t)total, (int64_t)g.la, (int64_t)g.lb, &bad);
+    if (bad && tid == 0) err_first(err, ERR_BAD_RUNS);
     const int nb = total - na;
     const uint64_t pa = g.pbase + (uint64_t)a0;
     const uint64_t pb = g.pbase + g.la + (d0 - (uint64_t)a0);
@@ -338,9 +349,11 @@ struct PairBulkShape {
 };
 
 // Geometry of output tile t, and the bulk loads of its slices into `stage`.
+// Splits that are inconsistent (runs that are not sorted) are clamped into
+// the runs and reported in *err (ERR_BAD_RUNS).
 template <class T, int TILE>
 __device__ __forceinline__ BulkTileGeom pair_bulk_issue(T* stage, const T* src, uint64_t n, uint64_t run,
-                                                        uint64_t t, int64_t s0, int64_t s1, uint64_t* bar) {
+                                                        uint64_t t, int64_t s0, int64_t s1, uint64_t* bar, int* err) {
     constexpr int V = Vec<T>::N;
     const uint64_t o = t * TILE;
     const PairGeom g(o, n, run);
@@ -350,7 +363,9 @@ __device__ __forceinline__ BulkTileGeom pair_bulk_issue(T* stage, const T* src, 
     const int64_t a1 = (o + TILE < g.pbase + pair_end) ? s1 : (int64_t)g.la;
     BulkTileGeom q;
     q.tile = t;
-    q.na = (int)(a1 - s0);
+    bool bad = false;
+    q.na = (int)tile_split(s0, a1, (int64_t)d0, (int64_t)(d1 - d0), (int64_t)g.la, (int64_t)g.lb, &bad);
+    if (bad) err_first(err, ERR_BAD_RUNS);
     q.nb = (int)(d1 - d0) - q.na;
     const uint64_t pa = g.pbase + (uint64_t)s0;
     const uint64_t pb = g.pbase + g.la + (d0 - (uint64_t)s0);
@@ -402,9 +417,11 @@ __global__ void __launch_bounds__(NT, MINB)
     // they take SM slots while this grid still merges, made a 1 GiB sort 25 %
     // slower.)
     grid_dep_wait();
+    // an earlier pass gave up on a wait: its output is not sorted, stop here
+    if (__syncthreads_or(tid == 0 && err_wait_set(err))) return;
     if (tid == 0) {
         const uint64_t t0 = blockIdx.x;
-        geom[0] = pair_bulk_issue<T, TILE>(stage(0), src, n, run, t0, splits[t0], splits[t0 + 1], &bar[0]);
+        geom[0] = pair_bulk_issue<T, TILE>(stage(0), src, n, run, t0, splits[t0], splits[t0 + 1], &bar[0], err);
         nt = claim_next();
         if (nt < num_tiles) {
             n0 = splits[nt];
@@ -421,7 +438,7 @@ __global__ void __launch_bounds__(NT, MINB)
         if (tid == 0) {
             if (nt < num_tiles) {
                 bulk_wait_read<0>();  // the other stage's last store has left shared memory
-                geom[s ^ 1] = pair_bulk_issue<T, TILE>(stage(s ^ 1), src, n, run, nt, n0, n1, &bar[s ^ 1]);
+                geom[s ^ 1] = pair_bulk_issue<T, TILE>(stage(s ^ 1), src, n, run, nt, n0, n1, &bar[s ^ 1], err);
             } else {
                 geom[s ^ 1].tile = num_tiles;
             }
