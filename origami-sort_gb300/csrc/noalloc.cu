@@ -57,12 +57,15 @@ int64_t* scratch_for(int dev, cudaError_t* err) {
     return g_scratch_ptr[dev];
 }
 
-uint64_t slots_needed(int kind, uint64_t n) {
+// Bytes of scratch a binary-pass sort of n items uses: its splitter slots
+// (rounded up to 256 bytes), then the 256-byte status tail whose first int is
+// the sort's error word.
+uint64_t scratch_needed(int kind, uint64_t n, uint64_t sort_n) {
     switch (kind) {
-        case ORIGAMI_U32: return merge_split_slots<uint32_t>(n);
+        case ORIGAMI_U32: return scratch_bytes_u32(n, sort_n, 2);
         case ORIGAMI_U64:
-        case ORIGAMI_I64: return merge_split_slots<uint64_t>(n);
-        default: return merge_split_slots<KV64>(n);
+        case ORIGAMI_I64: return scratch_bytes_u64(n, sort_n, 2);
+        default: return scratch_bytes_kv(n, sort_n, 2);
     }
 }
 
@@ -107,7 +110,7 @@ extern "C" int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_
         return noalloc_fail(ORIGAMI_ERR_NO_DEVICE, "no usable CUDA device");
     int64_t* scratch = scratch_for(dev, &e);
     if (!scratch) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
-    if (slots_needed(kind, n) > kSlots)  // defensive: implied by the limit above
+    if (scratch_needed(kind, n, sort_n) > sizeof(g_noalloc_scratch))  // defensive: implied by the limit above
         return noalloc_fail(ORIGAMI_ERR_INVALID, "n exceeds the no-alloc limit");
     const uint64_t m = (kind == ORIGAMI_I64 || kind == ORIGAMI_KV64) ? 0x8000000000000000ull : 0ull;
     void* want = in_tmp ? tmp : d;
@@ -120,11 +123,11 @@ extern "C" int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_
     }
     if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
     if (flags & ORIGAMI_FLAG_SYNC) {
-        // the sort's error word sits right after its splitter slots; the tile
-        // sort cleared it at the start of this call. The copy goes to the
-        // stack (the driver stages it; nothing is allocated).
+        // the sort's error word opens the 256-byte tail of the scratch it
+        // uses; the tile sort cleared it at the start of this call. The copy
+        // goes to the stack (the driver stages it; nothing is allocated).
         int word = 0;
-        e = cudaMemcpyAsync(&word, reinterpret_cast<const char*>(scratch) + slots_needed(kind, n) * sizeof(int64_t),
+        e = cudaMemcpyAsync(&word, reinterpret_cast<const char*>(scratch) + scratch_needed(kind, n, sort_n) - 256,
                             sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return noalloc_fail(ORIGAMI_ERR_CUDA, cudaGetErrorString(e));
