@@ -13,18 +13,25 @@
 //                   kway_split_kernel computes the exact split of every
 //                   run's super-samples at evenly spaced super-sample ranks;
 //  tiles (K4)     - kb_cut_kernel, one CTA per range: the range boundaries
-//                   are concrete super-samples, refined to exact sample and
-//                   item positions by one short search per run; the range's
-//                   samples are merged in shared memory and every M-th merged
-//                   sample becomes a tile cut, again refined to exact item
-//                   positions in each run by one search inside an S-item
-//                   block. A tile therefore holds at most (M + F) * S items
-//                   under any key distribution (every run contributes its
-//                   samples in the tile plus one partial block);
-//  merge (K3)     - kb_merge_kernel, persistent with claimed tiles: the F
-//                   slices of a tile arrive by cp.async.bulk (the 16-byte
-//                   chunks enclosing each slice) into one of two stages while
-//                   the other stage merges; log2(F) rounds of merge path merge
+//                   are concrete super-samples, refined to exact sample
+//                   positions by one short search per run in the sample
+//                   array; the range's samples are merged in shared memory and
+//                   every M-th merged sample becomes a tile cut. A cut is a
+//                   concrete item (the sample), stored with the number of
+//                   samples of every run at or before it, so its exact item
+//                   position in each run lies inside one S-item block;
+//  merge (K3)     - kb_merge_kernel, persistent with claimed tiles: for each
+//                   run the tile's samples plus the S-item block at either end
+//                   arrive by cp.async.bulk (the 16-byte chunks enclosing
+//                   them) into one of two stages while the other stage merges;
+//                   one search per run inside each boundary block, in shared
+//                   memory, gives the exact slices (the same search on the same
+//                   block in the tile on either side of a cut, so neighbouring
+//                   tiles agree). A tile therefore holds at most (M + F) * S
+//                   items under any key distribution (every run contributes its
+//                   samples in the tile plus one partial block), and no kernel
+//                   reads the runs outside the merge itself;
+//                   log2(F) rounds of merge path merge
 //                   the slices in place (every thread keeps its output block
 //                   in registers until all have read their inputs); the tile
 //                   leaves by one bulk store of its whole 16-byte chunks plus
@@ -159,17 +166,26 @@ __global__ void kb_gather_samples_kernel(const T* __restrict__ src, uint64_t n, 
 }
 
 // ------------------------------------------------------------- K4: cuts ---
-// One CTA per range (blockIdx.x = g * rpg + b). Writes tab[bid][c][k] for
-// c = 0 .. ntiles[bid]: the item offset in run k (from the run's start) of the
-// tile boundary c; tile c of the range is [tab[c][k], tab[c+1][k]) in every
-// run. bnd0 (rpg > 1): kway_split_kernel's super-sample counts per range
-// boundary, [g * (rpg+1) + b][KWAY_MAX]. The first CTA resets the merge
-// kernel's tile counter.
+// Cut table of the ranges of a pass: for range r, cuts c = 0 .. ntiles[r]
+// (c = 0 is the range's start; tile c lies between cuts c and c+1):
+//   q[r][c][k]  samples of run k at or before the cut (uint32)
+//   key[r][c]   the cut item's key (a sample of run run[r][c])
+//   run[r][c]   that run; -1: the group's start (all q = 0), -2: the group's
+//               end (every run to its last item)
+struct KbCuts {
+    uint32_t* q;
+    void* key;
+    int* run;
+};
+
+// One CTA per range (blockIdx.x = g * rpg + b): writes the range's cut table.
+// bnd0 (rpg > 1): kway_split_kernel's super-sample counts per range boundary,
+// [g * (rpg+1) + b][KWAY_MAX]. The first CTA resets the merge kernel's tile
+// counter.
 template <class T>
-__global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__ src,
-                                                          const typename Traits<T>::Key* __restrict__ samp,
+__global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits<T>::Key* __restrict__ samp,
                                                           uint64_t n, uint64_t run, int fan, int rpg,
-                                                          const int64_t* __restrict__ bnd0, int64_t* __restrict__ tab,
+                                                          const int64_t* __restrict__ bnd0, KbCuts cuts,
                                                           uint32_t* __restrict__ ntiles, unsigned* __restrict__ claim,
                                                           int* __restrict__ err) {
     using Sh = KbShape<T>;
@@ -183,11 +199,10 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__
     __shared__ int off[KWAY_MAX + 1];
     __shared__ int mblk[Sh::CUT_MAXBLK];
     __shared__ uint64_t qs[2][KWAY_MAX];  // sample co-ranks of the range's start / end cut
-    __shared__ uint64_t qi0[KWAY_MAX];    // item co-ranks of the start cut
-    __shared__ uint64_t rlen[KWAY_MAX], rns[KWAY_MAX];
+    __shared__ uint64_t rns[KWAY_MAX];
     __shared__ K cy[2];                   // keys of the start / end cut items
     __shared__ int cj[2];                 // their runs (-1: group start / group end)
-    __shared__ int ntl, cnt_all;
+    __shared__ int cnt_all;
     const int tid = threadIdx.x;
     const uint64_t bid = blockIdx.x;
     const uint64_t g = bid / (uint64_t)rpg;
@@ -199,11 +214,7 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__
         if (tid == 0) ntiles[bid] = 0;
         return;
     }
-    if (tid < KWAY_MAX) {
-        const uint64_t L = tid < fan ? grp.len(tid) : 0;
-        rlen[tid] = L;
-        rns[tid] = L / S;
-    }
+    if (tid < KWAY_MAX) rns[tid] = (tid < fan ? grp.len(tid) : 0) / S;
     __syncthreads();
     const uint64_t sbase = grp.base / S;  // group's first sample (runs start at multiples of S)
     const uint64_t rs = run / S;          // samples per full run
@@ -261,21 +272,6 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__
         }
         __syncthreads();
     }
-    // item co-ranks of the start cut
-    if (tid < KWAY_MAX) {
-        const int k = tid, j = cj[0];
-        uint64_t v = 0;
-        if (k < fan && j >= 0) {
-            if (k == j) {
-                v = qs[0][k] * S;
-            } else {
-                const uint64_t lo = qs[0][k] * S;
-                const uint64_t hi = min(lo + S - 1, rlen[k]);
-                v = kb_refine<T, K>(src + grp.start(k), lo, hi, cy[0], k < j);
-            }
-        }
-        qi0[k] = v;
-    }
     // --- the range's samples, tagged (index in range << 4 | run). For sorted
     // runs the end cut never precedes the start cut and a range holds at most
     // RANGE_SMAX samples; otherwise the range is reported and left empty.
@@ -321,10 +317,7 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__
     const bool last_range = (b == rpg - 1);
     const int nfull = cnt / M;
     const int nt = nfull + ((last_range || cnt % M) ? 1 : 0);  // tiles of this range
-    if (tid == 0) {
-        ntl = nt;
-        ntiles[bid] = (uint32_t)nt;
-    }
+    if (tid == 0) ntiles[bid] = (uint32_t)nt;
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) hist[q] = 0;
     __syncthreads();
     for (int x = tid; x < cnt; x += NT) atomicAdd(&hist[(x / M) * KWAY_MAX + (merged[x].tag & 15)], 1u);
@@ -338,30 +331,36 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const T* __restrict__
         }
     }
     __syncthreads();
-    int64_t* out = tab + bid * (uint64_t)(TPR + 1) * KWAY_MAX;
+    const uint64_t row = bid * (uint64_t)(TPR + 1);
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) {
         const int c = q / KWAY_MAX, k = q % KWAY_MAX;
         uint64_t v = 0;
         if (k >= fan) {
             v = 0;
         } else if (c == 0) {
-            v = qi0[k];
+            v = qs[0][k];
         } else if (c == nt && last_range) {
-            v = rlen[k];
+            v = rns[k];
         } else {
-            const int pos = (c == nt) ? cnt - 1 : c * M - 1;  // the cut sample
-            const E y = merged[pos];
-            const int j = (int)(y.tag & 15);
-            const uint64_t qk = qs[0][k] + hist[(c - 1) * KWAY_MAX + k];  // run-k samples up to the cut
-            if (k == j) {
-                v = qk * S;
-            } else {
-                const uint64_t lo = qk * S;
-                const uint64_t hi = min(lo + S - 1, rlen[k]);
-                v = kb_refine<T, K>(src + grp.start(k), lo, hi, y.key, k < j);
-            }
+            v = qs[0][k] + hist[(c - 1) * KWAY_MAX + k];  // run-k samples up to the cut
         }
-        out[q] = (int64_t)v;
+        cuts.q[row * KWAY_MAX + q] = (uint32_t)v;
+    }
+    for (int c = tid; c <= nt; c += NT) {
+        K y = 0;
+        int j;
+        if (c == 0) {
+            y = cy[0];
+            j = cj[0];
+        } else if (c == nt && last_range) {
+            j = -2;
+        } else {
+            const E e = merged[(c == nt) ? cnt - 1 : c * M - 1];  // the cut sample
+            y = e.key;
+            j = (int)(e.tag & 15);
+        }
+        static_cast<K*>(cuts.key)[row + c] = y;
+        cuts.run[row + c] = j;
     }
 }
 
@@ -437,27 +436,36 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
     }
 }
 
-// Geometry of a tile staged in shared memory (written by warp 0).
+// A tile staged in shared memory (written by warp 0).
 struct KbTileGeom {
     uint64_t slot;  // >= nslots: none (the CTA is done)
-    uint64_t o;     // first output item
-    int total;      // items
+    uint64_t g;     // its group
+    uint64_t o;     // first output item (after the boundary search)
+    int total;      // items (after the boundary search)
+};
+
+// Per-run state of a staged tile (lane k of warp 0 keeps run k's).
+struct KbSlice {
+    uint64_t a;  // first staged item, offset in the run
+    int lst;     // its stage index
+    int len;     // staged items
+    int dq;      // samples of the run in the tile: its end block starts at dq * S
 };
 
 // Persistent merge of every tile of the pass. Tiles are slots
 // [range * TPR + c]; a slot is a tile when c < ntiles[range]. A CTA starts
 // with slot blockIdx.x and claims later ones from *claim (reset by the cut
 // kernel), skipping slots that are no tile. Warp 0 stages the tiles: lane k
-// handles run k's slice (its geometry fetched one tile ahead), lane 0 the
-// claims and the barrier. samp_out / ssamp_out (may be null): samples of the
-// output for the next pass.
+// handles run k (its cut counts fetched one tile ahead), lane 0 the claims and
+// the barrier; once a tile has landed it finds the exact slice of each run by
+// one search in the block at each end. samp_out / ssamp_out (may be null):
+// samples of the output for the next pass.
 template <class T>
 __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
     kb_merge_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int fan, int rpg,
-                    const int64_t* __restrict__ tab, const uint32_t* __restrict__ ntiles, uint64_t nslots,
-                    uint64_t xout, typename Traits<T>::Key* __restrict__ samp_out,
-                    typename Traits<T>::Key* __restrict__ ssamp_out, unsigned* __restrict__ claim, int* err,
-                    uint32_t spin) {
+                    KbCuts cuts, const uint32_t* __restrict__ ntiles, uint64_t nslots, uint64_t xout,
+                    typename Traits<T>::Key* __restrict__ samp_out, typename Traits<T>::Key* __restrict__ ssamp_out,
+                    unsigned* __restrict__ claim, int* err, uint32_t spin) {
     using Sh = KbShape<T>;
     using C = KbCfg<T>;
     using K = typename Sh::K;
@@ -466,47 +474,62 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
     __shared__ int split[Sh::MAXBLK + 1];
     __shared__ int geo[2][2][2][KWAY_MAX];  // [stage][ping-pong][start, len][list]
     __shared__ KbTileGeom tg[2];
+    __shared__ KbSlice sl[2][KWAY_MAX];
+    __shared__ K cutk[2][2];                // [stage][start / end cut]: key
+    __shared__ int cutj[2][2];              // run of the cut item (-1 group start, -2 group end)
     __shared__ __align__(8) uint64_t bar[2];
     const int tid = threadIdx.x, lane = tid & 31;
     const uint64_t G = gridDim.x;
+    const K* ckey = static_cast<const K*>(cuts.key);
     auto stage = [&](int s) { return reinterpret_cast<T*>(smem_raw + (size_t)s * Sh::STAGE); };
     // warp 0 lane 0: the next slot that is a tile, from `t` on, claiming more
     auto next_tile = [&](uint64_t t) -> uint64_t {
         while (t < nslots && (uint32_t)(t % TPR) >= ntiles[t / TPR]) t = G + (uint64_t)atomicAdd(claim, 1u);
         return t;
     };
-    // warp 0 state: the slot staged next and lane k's slice of it in run k
+    // warp 0 state: the slot staged next, lane k's sample counts of run k at
+    // its two cuts, and the cut items
     uint64_t nslot = nslots;
-    int64_t na = 0, ne = 0;
+    uint32_t qa = 0, qe = 0;
+    K ya = 0, ye = 0;
+    int ja = -1, je = -2;
     auto fetch = [&](uint64_t t) {  // warp 0, uniform t
         nslot = t;
-        if (t < nslots && lane < KWAY_MAX) {
-            const int64_t* row = tab + (t / TPR) * (uint64_t)(TPR + 1) * KWAY_MAX + (t % TPR) * KWAY_MAX;
-            na = row[lane];
-            ne = row[KWAY_MAX + lane];
-        } else {
-            na = ne = 0;
+        if (t < nslots) {
+            const uint64_t row = (t / TPR) * (uint64_t)(TPR + 1) + t % TPR;  // cut c of the range
+            if (lane < KWAY_MAX) {
+                qa = cuts.q[row * KWAY_MAX + lane];
+                qe = cuts.q[(row + 1) * KWAY_MAX + lane];
+            }
+            ya = ckey[row];
+            ye = ckey[row + 1];
+            ja = cuts.run[row];
+            je = cuts.run[row + 1];
         }
     };
-    // warp 0: stage the fetched tile into stage s (barrier bar[s])
+    // warp 0: stage the fetched tile into stage s (barrier bar[s]): for run k
+    // the items from the block of cut c (its start, or the run's start at a
+    // group start) to the end of the block of cut c+1 (or the run's end)
     auto issue = [&](int s) {
         const bool any = nslot < nslots;
         const uint64_t g = nslot / TPR / (uint64_t)rpg;
-        const uint64_t abs = g * run * (uint64_t)fan + (uint64_t)lane * run + (uint64_t)na;  // slice start
-        // a tile of sorted runs has slices of 0 .. TMAX items inside their runs
-        // and at most TMAX in all; anything else (runs that are not sorted) is
-        // reported and the tile is left out
         const bool mine = lane < fan && any;
-        const int64_t l64 = mine ? ne - na : 0;
         const uint64_t rs = g * run * (uint64_t)fan + (uint64_t)lane * run;  // run start
-        const int64_t rl = mine ? (int64_t)(rs >= n ? 0 : (n - rs < run ? n - rs : run)) : 0;
-        const bool inside = !mine || (l64 >= 0 && l64 <= Sh::TMAX && na >= 0 && ne <= rl);
-        int tl = inside ? (int)l64 : 0;
+        const uint64_t rl = mine ? (rs >= n ? 0 : (n - rs < run ? n - rs : run)) : 0;
+        const uint64_t a = (ja < 0) ? 0 : (uint64_t)qa * S;
+        uint64_t e = (je == -2) ? rl : (uint64_t)qe * S + S - 1;
+        e = e < rl ? e : rl;
+        // staged slices of sorted runs lie in their runs and hold at most TMAX
+        // items in all; anything else (runs that are not sorted) is reported
+        // and the tile is left out
+        const bool inside = !mine || (a <= e && e - a <= (uint64_t)Sh::TMAX && qe >= qa);
+        int tl = (inside && mine) ? (int)(e - a) : 0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) tl += __shfl_xor_sync(0xFFFFFFFFu, tl, o);
         const bool bad = __any_sync(0xFFFFFFFFu, !inside) || tl > Sh::TMAX;
         if (bad && lane == 0) err_first(err, ERR_BAD_RUNS);
-        const int len = bad ? 0 : (int)l64;
+        const int len = (mine && !bad) ? (int)(e - a) : 0;
+        const uint64_t abs = rs + a;
         const int lead = len > 0 ? (int)(abs % V) : 0;
         const int nv = len > 0 ? (lead + len + V - 1) / V : 0;
         // exclusive prefix of the slices' vectors over the lanes
@@ -518,25 +541,68 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
         }
         const int total_v = __shfl_sync(0xFFFFFFFFu, pre, 31);
         const int voff = pre - nv;
-        int tot = len;
-        uint64_t o0 = (uint64_t)na;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
-            o0 += __shfl_xor_sync(0xFFFFFFFFu, o0, o);
-        }
         if (lane < KWAY_MAX) {
-            geo[s][0][0][lane] = voff * V + lead;
-            geo[s][0][1][lane] = len;
+            KbSlice v;
+            v.a = mine ? a : 0;
+            v.lst = voff * V + lead;
+            v.len = len;
+            v.dq = (mine && !bad) ? (int)(qe - qa) : 0;
+            sl[s][lane] = v;
         }
         if (lane == 0) {
             tg[s].slot = any ? nslot : nslots;
-            tg[s].o = g * run * (uint64_t)fan + o0;
-            tg[s].total = tot;
+            tg[s].g = g;
+            cutk[s][0] = ya;
+            cutk[s][1] = ye;
+            cutj[s][0] = bad ? -1 : ja;
+            cutj[s][1] = bad ? -2 : je;
             if (any) mbar_arrive_expect(&bar[s], (uint32_t)total_v * 16u);
         }
         __syncwarp();
         if (any && nv > 0) bulk_load(stage(s) + voff * V, src + (abs - lead), (uint32_t)nv * 16u, &bar[s]);
+    };
+    // warp 0, after stage s has landed: exact slices. Run k starts after the
+    // items of its first block that precede the start cut and ends after the
+    // items of its last block that precede the end cut (items of earlier runs
+    // precede an equal key, later ones follow; the cut's own run is exact).
+    auto bounds = [&](int s) {
+        const T* buf = stage(s);
+        int b = 0, e = 0;
+        uint64_t a = 0;
+        if (lane < fan) {
+            const KbSlice v = sl[s][lane];
+            const int j0 = cutj[s][0], j1 = cutj[s][1];
+            const T* p = buf + v.lst;
+            if (j0 >= 0 && lane != j0) b = (int)kb_refine<T, K>(p, 0, (uint64_t)min(S - 1, v.len), cutk[s][0], lane < j0);
+            if (j1 == -2 || v.len == 0) {
+                e = v.len;
+            } else {
+                const int base = min(v.dq * S, v.len);
+                e = (lane == j1) ? base
+                                 : (int)kb_refine<T, K>(p, base, (uint64_t)min(base + S - 1, v.len), cutk[s][1],
+                                                        lane < j1);
+            }
+            if (e < b) {  // cannot happen for sorted runs
+                err_first(err, ERR_BAD_RUNS);
+                e = b;
+            }
+            a = v.a + (uint64_t)b;
+            geo[s][0][0][lane] = v.lst + b;
+            geo[s][0][1][lane] = e - b;
+        } else if (lane < KWAY_MAX) {
+            geo[s][0][0][lane] = 0;
+            geo[s][0][1][lane] = 0;
+        }
+        int tot = e - b;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tot += __shfl_xor_sync(0xFFFFFFFFu, tot, o);
+            a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+        }
+        if (lane == 0) {
+            tg[s].o = tg[s].g * run * (uint64_t)fan + a;
+            tg[s].total = tot;
+        }
     };
 
     if (tid == 0) {
@@ -559,8 +625,7 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
     __syncthreads();
     uint32_t phase = 0;  // bit s: parity of stage s's next completion
     for (int s = 0;; s ^= 1) {
-        const KbTileGeom q = tg[s];
-        if (q.slot >= nslots) break;
+        if (tg[s].slot >= nslots) break;
         // warp 0 stages the next tile into the other stage (its previous bulk
         // store has left shared memory), then fetches the one after
         if (tid < 32) {
@@ -579,6 +644,9 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
             return;
         }
         phase ^= 1u << s;
+        if (tid < 32) bounds(s);
+        __syncthreads();
+        const KbTileGeom q = tg[s];
         T* buf = stage(s);
         const int sh = (int)(q.o % V);  // stage index x holds output item q.o + x - sh
         kb_merge_tile<T, NT, C::VT, Sh::STABLE>(buf, geo[s], fan, sh, xout, split);

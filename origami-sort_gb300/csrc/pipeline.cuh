@@ -243,7 +243,7 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
 //   splits     binary passes: one int64 per merge tile + 2
 //   k-way passes (only when the plan has some, kway_bulk.cuh):
 //   bnd0       super-sample splits of the range boundaries, [groups][rpg+1][16]
-//   tab        tile cuts, [ranges][TPR+1][16] int64
+//   cut q/key/run  the ranges' tile cuts (KbCuts), [ranges][TPR+1]([16])
 //   ntiles     tiles per range
 //   samp 0/1   samples (one key per S items) of the runs a pass reads / writes
 //   ssamp 0/1  super-samples (one key per S*64 items)
@@ -254,7 +254,7 @@ struct PipeScratch {
     uint64_t bytes = 0;  // total, tail included
     int64_t* splits = nullptr;
     int64_t* bnd0 = nullptr;
-    int64_t* tab = nullptr;
+    KbCuts cuts{nullptr, nullptr, nullptr};
     uint32_t* ntiles = nullptr;
     K* samp[2] = {nullptr, nullptr};
     K* ssamp[2] = {nullptr, nullptr};
@@ -268,21 +268,22 @@ struct PipeScratch {
             o += (sz + 255) & ~255ull;
             return r;
         };
-        uint64_t bnd_b = 0, tab_b = 0, rng = 0;
+        uint64_t bnd_b = 0, rng = 0;
         bool kway = false;
         for (const PassPlan& p : plan_passes<T>(n, chunk_limit(n, sort_n), shape_fan(code), start_run)) {
             if (p.fan <= 2) continue;
             kway = true;
-            const uint64_t r = p.groups * (uint64_t)p.rpg;
             if (p.rpg > 1) bnd_b = std::max<uint64_t>(bnd_b, p.groups * (uint64_t)(p.rpg + 1) * KWAY_MAX * 8);
-            tab_b = std::max<uint64_t>(tab_b, r * (uint64_t)(KbShape<T>::TPR + 1) * KWAY_MAX * 8);
-            rng = std::max<uint64_t>(rng, r);
+            rng = std::max<uint64_t>(rng, p.groups * (uint64_t)p.rpg);
         }
         splits = reinterpret_cast<int64_t*>(take(merge_split_slots<T>(n) * sizeof(int64_t)));
         if (kway) {
             constexpr uint64_t S = KbCfg<T>::S;
+            const uint64_t rows = rng * (uint64_t)(KbShape<T>::TPR + 1);
             if (bnd_b) bnd0 = reinterpret_cast<int64_t*>(take(bnd_b));
-            tab = reinterpret_cast<int64_t*>(take(tab_b));
+            cuts.q = reinterpret_cast<uint32_t*>(take(rows * KWAY_MAX * 4));
+            cuts.key = take(rows * sizeof(K));
+            cuts.run = reinterpret_cast<int*>(take(rows * 4));
             ntiles = reinterpret_cast<uint32_t*>(take(rng * 4));
             for (int i = 0; i < 2; ++i) samp[i] = reinterpret_cast<K*>(take((n / S + 1) * sizeof(K)));
             for (int i = 0; i < 2; ++i) ssamp[i] = reinterpret_cast<K*>(take((n / (S * KB_SS) + 1) * sizeof(K)));
@@ -463,13 +464,13 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
             const uint64_t ranges = p.groups * (uint64_t)p.rpg;
             launch(n_kc.c_str(), st, [&] {
                 kb_cut_kernel<T><<<(unsigned)ranges, KB_CUT_NT, KbShape<T>::CUT_SMEM, st>>>(
-                    cur, s_in, n, p.run, p.fan, p.rpg, sc.bnd0, sc.tab, sc.ntiles, claim, err);
+                    s_in, n, p.run, p.fan, p.rpg, sc.bnd0, sc.cuts, sc.ntiles, claim, err);
             });
             const uint64_t nslots = ranges * (uint64_t)KbShape<T>::TPR;
             const uint64_t grid = std::min<uint64_t>(nslots, kb_resident<T>());
             launch(n_km.c_str(), st, [&] {
                 kb_merge_kernel<T><<<(unsigned)grid, KbCfg<T>::NT, KbShape<T>::SMEM, st>>>(
-                    cur, nxt, n, p.run, p.fan, p.rpg, sc.tab, sc.ntiles, nslots, xo, s_out, ss_out, claim, err,
+                    cur, nxt, n, p.run, p.fan, p.rpg, sc.cuts, sc.ntiles, nslots, xo, s_out, ss_out, claim, err,
                     wait_limit());
             });
             if (stats) stats->kernels += 2;
