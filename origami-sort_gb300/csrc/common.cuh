@@ -195,29 +195,23 @@ __device__ __forceinline__ int64_t global_merge_path_interp(const T* A, int64_t 
     return lo;
 }
 
-// Slice of run A that one merge tile takes: the tile covers outputs [d0, d0 +
+// Items of run A that one merge tile takes: the tile covers outputs [d0, d0 +
 // total) of the pair (A of la items, B of lb), s0 and a1 are the merge-path
-// splits at its two ends. For sorted runs the splits are consistent and this
-// returns a1 - s0 unchanged. Otherwise (runs that are not sorted) s0 and the
-// count are clamped so that both slices lie inside their runs and hold
-// `total` items between them, and *bad is set: every access stays in bounds
-// whatever the data.
-__device__ __forceinline__ int64_t tile_split(int64_t& s0, int64_t a1, int64_t d0, int64_t total, int64_t la,
-                                              int64_t lb, bool* bad) {
-    const int64_t slo = d0 - lb > 0 ? d0 - lb : 0, shi = d0 < la ? d0 : la;
-    if (s0 < slo || s0 > shi) {
-        *bad = true;
-        s0 = s0 < slo ? slo : shi;
-    }
-    int64_t na = a1 - s0;
-    const int64_t lo0 = total - (lb - (d0 - s0));
-    const int64_t lo = lo0 > 0 ? lo0 : 0;
-    const int64_t hi = total < la - s0 ? total : la - s0;
-    if (na < lo || na > hi) {
-        *bad = true;
-        na = na < lo ? lo : hi;
-    }
-    return na;
+// splits at its two ends (each from a bounded search, so s0 lies in [max(0,
+// d0-lb), min(d0, la)]). For sorted runs the splits are consistent and a1 - s0
+// is returned unchanged. Otherwise (runs that are not sorted) the count is
+// clamped so that both slices lie inside their runs, and *bad is set: every
+// access stays in bounds whatever the data.
+__device__ __forceinline__ int tile_split(int64_t s0, int64_t a1, int64_t d0, int total, int64_t la, int64_t lb,
+                                          bool* bad) {
+    const int64_t na = a1 - s0;
+    const int64_t lo = (int64_t)total - (lb - (d0 - s0));
+    const int64_t hi = la - s0;
+    int64_t c = na < lo ? lo : na;
+    c = c > hi ? hi : c;
+    c = c < 0 ? 0 : (c > total ? total : c);
+    *bad = c != na;
+    return (int)c;
 }
 
 // 16-byte vector view of items (all buffers the kernels touch are 16-byte

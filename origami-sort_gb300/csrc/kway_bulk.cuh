@@ -137,16 +137,18 @@ __device__ __forceinline__ uint64_t kb_refine(const T* a, uint64_t lo, uint64_t 
 // Samples of a sorted tile of `valid` items held in shared memory (`tile`,
 // unpadded) whose first item is global item `base` (a multiple of S): called
 // by the tile sort, every thread of the CTA (nthr of them).
+// (A tile holds a whole number of super-samples: base is a multiple of S*SS.)
 template <class T>
 __device__ __forceinline__ void kb_emit_samples(const T* tile, uint64_t base, int valid,
                                                 typename Traits<T>::Key* samp, typename Traits<T>::Key* ssamp,
                                                 int nthr) {
     constexpr int S = KbCfg<T>::S;
+    typename Traits<T>::Key* sp = samp + base / S;
+    typename Traits<T>::Key* ssp = ssamp + base / (S * KB_SS);
     for (int j = threadIdx.x; j < valid / S; j += nthr) {
-        const uint64_t i = base / S + (uint64_t)j;
-        const auto k = Traits<T>::key(tile[(j + 1) * S - 1]);
-        samp[i] = k;
-        if (i % KB_SS == KB_SS - 1) ssamp[i / KB_SS] = k;
+        const auto k = Traits<T>::key(tile[j * S + S - 1]);
+        sp[j] = k;
+        if ((j & (KB_SS - 1)) == KB_SS - 1) ssp[j / KB_SS] = k;
     }
 }
 
@@ -299,15 +301,18 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits
     }
     __syncthreads();
     const int cnt = cnt_all;
-    for (int k = 0; k < fan; ++k) {
-        const int c = off[k + 1] - off[k];
-        const K* sp = samp + sbase + (uint64_t)k * rs + qs[0][k];
-        for (int i = tid; i < c; i += NT) {
-            E e;
-            e.key = sp[i];
-            e.tag = ((uint32_t)i << 4) | (uint32_t)k;
-            sA[off[k] + i] = e;
-        }
+    // one flat pass over the range's samples: item x belongs to the run k with
+    // off[k] <= x < off[k+1] (all loads independent)
+#pragma unroll 4
+    for (int x = tid; x < cnt; x += NT) {
+        int k = 0;
+#pragma unroll
+        for (int q = 1; q < KWAY_MAX; ++q) k += (off[q] <= x) ? 1 : 0;
+        const int i = x - off[k];
+        E e;
+        e.key = samp[sbase + (uint64_t)k * rs + qs[0][k] + (uint64_t)i];
+        e.tag = ((uint32_t)i << 4) | (uint32_t)k;
+        sA[x] = e;
     }
     __syncthreads();
     E* merged = sA;
@@ -396,22 +401,31 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
             }
         }
         int a0 = 0, la = 0, b0 = 0, lb = 0, diag = 0;
+        T r[VT];
+        int cnt = 0;
         if (p >= 0) {
             a0 = lst[2 * p];
             la = len[2 * p];
             b0 = lst[2 * p + 1];
             lb = len[2 * p + 1];
             diag = (tid - first) * VO;
-            split[tid] = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
-        }
-        __syncthreads();
-        T r[VT];
-        int cnt = 0;
-        if (p >= 0) {
             cnt = min(VO, la + lb - diag);
-            const int sa = split[tid];
-            const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
-            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
+        }
+        if constexpr (STABLE) {
+            // serial merge of the block: its end split comes from the next block
+            if (p >= 0) split[tid] = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
+            __syncthreads();
+            if (p >= 0) {
+                const int sa = split[tid];
+                const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
+                merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
+            }
+        } else {
+            // windows from the block's own split: no exchange of splits
+            if (p >= 0) {
+                const int sa = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
+                merge_window_regs<T, VT>(buf, a0, la, b0, lb, sa, diag, r);
+            }
         }
         // next round's geometry (the other buffer; nothing reads it this round)
         if (tid < npairs) {
@@ -422,13 +436,17 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
         if (p >= 0) {
             T* w = buf + (last ? out0 : a0) + diag;
             const uint64_t x = last ? xo : 0;
+            if (x) {
+#pragma unroll
+                for (int i = 0; i < VO; ++i) r[i] = Traits<T>::flip(r[i], x);
+            }
             if (cnt == VO) {
 #pragma unroll
-                for (int i = 0; i < VO; ++i) w[i] = Traits<T>::flip(r[i], x);
+                for (int i = 0; i < VO; ++i) w[i] = r[i];
             } else {
 #pragma unroll
                 for (int i = 0; i < VO; ++i)
-                    if (i < cnt) w[i] = Traits<T>::flip(r[i], x);
+                    if (i < cnt) w[i] = r[i];
             }
         }
         __syncthreads();

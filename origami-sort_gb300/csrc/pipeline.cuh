@@ -350,10 +350,12 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
 
     // kernel attributes, once per process (thread-safe static initialisation)
     static const bool configured = [] {
-        if constexpr (C::WARP_K1)
+        if constexpr (C::WARP_K1) {
             cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
-        else
+            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
+        } else
             cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         PairMerge1<T>::configure();
@@ -402,11 +404,16 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     if (!start_run) {
         T* k1_out = written_by(0);
         launch(n_k1.c_str(), st, [&] {
-            if constexpr (C::WARP_K1)
-                warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
-                    <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
-                        in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err, k1_samp, k1_ssamp);
-            else
+            if constexpr (C::WARP_K1) {
+                if (k1_samp)
+                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true>
+                        <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
+                            in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err, k1_samp, k1_ssamp);
+                else
+                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
+                        <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
+                            in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err);
+            } else
                 block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>
                     <<<(unsigned)tiles1, C::K1_NT, k1_smem<T>(), st>>>(in, k1_out, n, k1_chunk, xin,
                                                                        passes == 0 ? xout : 0, err, k1_samp,

@@ -421,8 +421,8 @@ __device__ __forceinline__ SegBulkGeom seg_bulk_issue(T* stage, const T* d, cons
     SegBulkGeom q;
     q.job = j;
     q.flags = r.la_flags;
-    bool bad = false;
-    q.na = (int)tile_split(s0, a1, (int64_t)r.d0, (int64_t)(r.d1 - r.d0), (int64_t)la, (int64_t)r.lb, &bad);
+    bool bad;
+    q.na = tile_split(s0, a1, (int64_t)r.d0, (int)(r.d1 - r.d0), (int64_t)la, (int64_t)r.lb, &bad);
     if (bad) err_first(err, ERR_BAD_RUNS);
     q.nb = (int)(r.d1 - r.d0) - q.na;
     q.obase = r.base + r.d0;
@@ -515,15 +515,21 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         T* buf = stage(s);
         const int tot = q.na + q.nb;
         const int nblk = (tot + VO - 1) / VO;
-        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
-        __syncthreads();
         T r[C::P_VT];
         const int diag = tid * VO;
         const int cnt = tid < nblk ? min(VO, tot - diag) : 0;
-        if (tid < nblk) {
-            const int sa = split[tid];
-            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+        if constexpr (C::STABLE) {
+            if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
+            __syncthreads();
+            if (tid < nblk) {
+                const int sa = split[tid];
+                const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+                merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+            }
+        } else if (tid < nblk) {
+            // keys: windows at the block's own split (merge_core.cuh)
+            const int sa = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
+            merge_window_regs<T, C::P_VT>(buf, q.as, q.na, q.bs, q.nb, sa, diag, r);
         }
         __syncthreads();
         // stage index x holds output item x - sh, so x = 0 lies on a 16-byte

@@ -117,8 +117,10 @@ struct WarpSortShape {
 // `ahead` > 0: the CTA first asks for the tile `ahead` places further on to be
 // brought into L2 (the tile a CTA of the next wave will load), so that later
 // CTAs find their keys in L2. err (optional): the sort's error word, cleared by
-// the first thread.
-template <class T, int NW, int VT, int NWT = NW, int MINB = 1>
+// the first thread. SAMPLES: also writes the samples of the sorted tiles to
+// samp / ssamp for a k-way pass that follows (kway_bulk.cuh); a separate
+// instantiation, so that the plain tile sort keeps its registers.
+template <class T, int NW, int VT, int NWT = NW, int MINB = 1, bool SAMPLES = false>
 __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T* __restrict__ in,
                                                                         T* __restrict__ out, uint64_t n,
                                                                         int chunk, uint64_t xin,
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
             *reinterpret_cast<uint4*>(out + base + (size_t)i * V) = *reinterpret_cast<const uint4*>(e);
         }
         for (int i = nvec * V + tid; i < valid; i += Sh::NTM) out[base + i] = Traits<T>::flip(src[i], xout);
-        if (samp) kb_emit_samples<T>(src, base, valid, samp, ssamp, Sh::NTM);
+        if constexpr (SAMPLES) kb_emit_samples<T>(src, base, valid, samp, ssamp, Sh::NTM);
     } else if (sorter) {
         // runs end at the warp (or chunk) size: each lane stores its own keys
         const int i0 = w0 + lane * VT;
@@ -293,11 +295,11 @@ __global__ void __launch_bounds__(NT, MINB) pair_merge_kernel(const T* __restric
     const uint64_t pair_end = g.la + g.lb;
     const uint64_t d1 = (d0 + TILE) < pair_end ? (d0 + TILE) : pair_end;
     if (__syncthreads_or(tid == 0 && err_wait_set(err))) return;  // an earlier pass gave up
-    int64_t a0 = splits[t];
+    const int64_t a0 = splits[t];
     const int64_t a1 = (o + TILE < g.pbase + pair_end) ? splits[t + 1] : (int64_t)g.la;
     const int total = (int)(d1 - d0);
-    bool bad = false;
-    const int na = (int)tile_split(a0, a1, (int64_t)d0, (int64_t)total, (int64_t)g.la, (int64_t)g.lb, &bad);
+    bool bad;
+    const int na = tile_split(a0, a1, (int64_t)d0, total, (int64_t)g.la, (int64_t)g.lb, &bad);
     if (bad && tid == 0) err_first(err, ERR_BAD_RUNS);
     const int nb = total - na;
     const uint64_t pa = g.pbase + (uint64_t)a0;
@@ -363,8 +365,8 @@ __device__ __forceinline__ BulkTileGeom pair_bulk_issue(T* stage, const T* src, 
     const int64_t a1 = (o + TILE < g.pbase + pair_end) ? s1 : (int64_t)g.la;
     BulkTileGeom q;
     q.tile = t;
-    bool bad = false;
-    q.na = (int)tile_split(s0, a1, (int64_t)d0, (int64_t)(d1 - d0), (int64_t)g.la, (int64_t)g.lb, &bad);
+    bool bad;
+    q.na = tile_split(s0, a1, (int64_t)d0, (int)(d1 - d0), (int64_t)g.la, (int64_t)g.lb, &bad);
     if (bad) err_first(err, ERR_BAD_RUNS);
     q.nb = (int)(d1 - d0) - q.na;
     const uint64_t pa = g.pbase + (uint64_t)s0;
@@ -463,15 +465,21 @@ __global__ void __launch_bounds__(NT, MINB)
         // one merge round, outputs kept in registers until every thread has
         // read its inputs, then written back over the stage
         const int nblk = (total + VO - 1) / VO;
-        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
-        __syncthreads();
         T r[VT];
         const int diag = tid * VO;
         const int cnt = tid < nblk ? min(VO, total - diag) : 0;
-        if (tid < nblk) {
-            const int sa = split[tid];
-            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+        if constexpr (STABLE) {
+            if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
+            __syncthreads();
+            if (tid < nblk) {
+                const int sa = split[tid];
+                const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+                merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+            }
+        } else if (tid < nblk) {
+            // keys: windows at the block's own split (merge_core.cuh)
+            const int sa = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
+            merge_window_regs<T, VT>(buf, q.as, q.na, q.bs, q.nb, sa, diag, r);
         }
         __syncthreads();
         if (cnt == VO) {
