@@ -239,7 +239,10 @@ def short_workloads(torch):
             top = ok[-1]
             out["latency"] = {"p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
                               "offered_rate_per_s": top["offered_rate"],
-                              "keys_per_s": top["keys_per_s"], "source": "serving loop"}
+                              "keys_per_s": top["keys_per_s"], "source": "serving loop",
+                              # the largest request's own copies in and out at the measured link rate
+                              "largest_request_link_floor_ms": sv.get("largest_request", {}).get("link_floor_ms"),
+                              "saturation_vs_loop_plain": sv.get("saturation_vs_loop_plain")}
     except Exception as e:
         out["serving"] = {"error": repr(e)}
     return out

@@ -433,6 +433,9 @@ cudaError_t typed_kway_final(int kind, const void* in, void* out, uint64_t n, ui
     }
 }
 
+// Scratch bytes of kway_pass_sliced (the final pass of the chunked host pipeline).
+uint64_t kway_final_bytes(int kind, uint64_t n);
+
 // Byte offset of the error word in kway_pass_sliced's scratch.
 uint64_t typed_kway_final_err(int kind, uint64_t n) {
     switch (kind) {
@@ -442,6 +445,8 @@ uint64_t typed_kway_final_err(int kind, uint64_t n) {
         default: return kway_final_err_kv(n);
     }
 }
+
+uint64_t kway_final_bytes(int kind, uint64_t n) { return typed_kway_final_err(kind, n) + 256; }
 
 // Copies each finished slice of the final pass to the host on the copy stream.
 struct SliceCopy {
@@ -464,47 +469,83 @@ struct SliceCopy {
     }
 };
 
-int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n,
-                     uint64_t sort_n, unsigned min_k, cudaStream_t st) {
+// The host pipeline's plan: whether it runs chunked, the pass shapes, and the
+// device memory it takes from one block (each part 256-byte aligned).
+struct HostPipePlan {
+    bool chunked = false;
+    uint64_t chunk_n = 0;
+    int fan = 0, cfan = 0, mfan = 0;
+    uint64_t data = 0, ws = 0, wm = 0, total = 0;  // A and B (data each), lane scratch, merge scratch
+};
+
+uint64_t a256(uint64_t b) { return (b + 255) & ~255ull; }
+
+HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_k) {
+    HostPipePlan p;
+    const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
+    p.fan = shape_for(kind, n, min_k);
+    p.chunk_n = 1ull << 22;
+    while (p.chunk_n * 16 <= n) p.chunk_n <<= 1;  // 8 to 16 chunks (4 and 16 measured slower at 1 GiB)
+    p.chunked = n >= 4 * p.chunk_n && limit > p.chunk_n;
+    p.data = a256(n * item_bytes(kind));
+    if (!p.chunked) {
+        p.ws = a256(typed_scratch_io(kind, n, sort_n, p.fan, 0));
+        p.total = 2 * p.data + p.ws;
+        return p;
+    }
+    // chunks sort on HOST_LANES-1 streams at once; binary passes use the
+    // one-tile-per-CTA merge shape, whose launches from the different streams
+    // interleave (one chunk's splitter searches overlap another's merges; 8
+    // chunk sorts of 2^25 keys: 6.97 ms on 4 streams against 8.3 ms for the
+    // persistent kernels on one)
+    p.cfan = shape_for(kind, p.chunk_n, min_k);  // the chunks' own tuned shape
+    if (shape_fan(p.cfan) == 2) p.cfan = shape_code(2, 2);
+    p.ws = a256(typed_scratch_io(kind, p.chunk_n, 0, p.cfan, 0));
+    // the merges across chunks are one k-way pass: bound by the host link it
+    // writes (1 GiB in ~5.6 ms), which hides its cost per level
+    const uint64_t need = (limit + p.chunk_n - 1) / p.chunk_n;
+    p.mfan = 2;
+    while ((uint64_t)p.mfan < need && p.mfan < 16) p.mfan <<= 1;
+    p.wm = a256(std::max(typed_scratch_io(kind, n, sort_n, p.mfan, p.chunk_n), kway_final_bytes(kind, n)));
+    p.total = 2 * p.data + (HOST_LANES - 1) * p.ws + p.wm;
+    return p;
+}
+
+// Sorts n items from `host_in` into `host_out` (host memory the device can
+// address through vin / vout, or device memory) with the memory of one block
+// of plan.total bytes, on `st` and this thread's helper streams; returns when
+// the result is in place. Large sorts are cut into chunks: each chunk arrives
+// in HBM (a copy-engine transfer for pinned memory, else the first kernel's
+// own reads) and is sorted on one of four streams while the next chunks are in
+// flight; the merge across chunks follows as one k-way pass, cut into output
+// slices that go to pinned host output while the next slices merge (or
+// writing the host output directly). Small sorts run one pipeline whose first
+// kernel reads the input and whose last pass writes the output.
+int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n, uint64_t sort_n,
+                  const HostPipePlan& p, void* block, cudaStream_t st) {
     const uint64_t ib = item_bytes(kind);
-    const uint64_t bytes = n * ib;
-    const int fan = shape_for(kind, n, min_k);
     const uint64_t m = key_mask(kind);
     const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
-    uint64_t chunk_n = 1ull << 22;
-    while (chunk_n * 16 <= n) chunk_n <<= 1;  // 8 to 16 chunks (4 and 16 measured slower at 1 GiB)
-    const bool chunked = shape_fan(fan) == 2 && n >= 4 * chunk_n && limit > chunk_n;
-    void *A = nullptr, *B = nullptr, *wm = nullptr;
-    void* w[HOST_LANES] = {};
+    char* blk = static_cast<char*>(block);
+    char* a = blk;
+    char* b = blk + p.data;
     ErrWatch watch;  // every sort's error word, read after the final sync
-    CK(cudaMallocAsync(&A, bytes, st), "arena allocation");
-    cudaError_t e = cudaMallocAsync(&B, bytes, st);
-    if (!chunked) {
-        const uint64_t ws = typed_scratch_io(kind, n, sort_n, fan, 0);
-        if (e == cudaSuccess) e = cudaMallocAsync(&w[0], ws, st);
-        if (e == cudaSuccess) e = typed_io(kind, vin, vout, A, B, n, sort_n, m, m, 0, fan, w[0], st);
-        if (e == cudaSuccess) e = watch.watch(static_cast<char*>(w[0]) + ws - 256, st);
+    cudaError_t e = cudaSuccess;
+    std::vector<cudaEvent_t> evs;
+    if (!p.chunked) {
+        void* w = b + p.data;
+        e = typed_io(kind, vin, vout, a, b, n, sort_n, m, m, 0, p.fan, w, st);
+        if (e == cudaSuccess)
+            e = watch.watch(static_cast<char*>(w) + typed_scratch_io(kind, n, sort_n, p.fan, 0) - 256, st);
     } else {
-        // chunks sort on HOST_LANES-1 streams at once; binary passes use the
-        // one-tile-per-CTA merge shape, whose launches from the different
-        // streams interleave (one chunk's splitter searches overlap another's
-        // merges; 8 chunk sorts of 2^25 keys: 6.97 ms on 4 streams against
-        // 8.3 ms for the persistent kernels on one)
-        int cfan = shape_for(kind, chunk_n, min_k);  // the chunks' own tuned shape
-        if (shape_fan(cfan) == 2) cfan = shape_code(2, 2);
-        const uint64_t cs = typed_scratch_io(kind, chunk_n, 0, cfan, 0);
-        for (int i = 0; i < HOST_LANES - 1 && e == cudaSuccess; ++i) e = cudaMallocAsync(&w[i], cs, st);
-        // the merges across chunks are one k-way pass: bound by the host link
-        // it writes (1 GiB in ~5.6 ms), which hides its cost per level
-        const uint64_t need = (limit + chunk_n - 1) / chunk_n;
-        int mfan = 2;
-        while ((uint64_t)mfan < need && mfan < 16) mfan <<= 1;
-        if (e == cudaSuccess) e = cudaMallocAsync(&wm, typed_scratch_io(kind, n, sort_n, mfan, chunk_n), st);
+        const uint64_t chunk_n = p.chunk_n;
+        char* w[HOST_LANES - 1];
+        for (int i = 0; i < HOST_LANES - 1; ++i) w[i] = b + p.data + (uint64_t)i * p.ws;
+        char* wm = b + p.data + (HOST_LANES - 1) * p.ws;
         const bool copy_in = is_pinned(host_in);
         cudaStream_t lanes[HOST_LANES - 1] = {st};
         for (int i = 1; i < HOST_LANES - 1; ++i) lanes[i] = aux_stream(i - 1);
         cudaStream_t sc = aux_stream(HOST_LANES - 1);
-        std::vector<cudaEvent_t> evs;
         auto event_on = [&](cudaStream_t s) {
             cudaEvent_t ev;
             cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -512,13 +553,9 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
             evs.push_back(ev);
             return ev;
         };
-        if (e == cudaSuccess) {
-            const cudaEvent_t ready = event_on(st);  // buffers allocated
-            for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(lanes[i], ready, 0);
-            cudaStreamWaitEvent(sc, ready, 0);
-        }
-        char* a = static_cast<char*>(A);
-        char* b = static_cast<char*>(B);
+        const cudaEvent_t ready = event_on(st);  // the block's earlier users are done
+        for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(lanes[i], ready, 0);
+        cudaStreamWaitEvent(sc, ready, 0);
         for (uint64_t off = 0, c = 0; e == cudaSuccess && off < n; off += chunk_n, ++c) {
             const uint64_t cn = n - off < chunk_n ? n - off : chunk_n;
             const int lane = (int)(c % (HOST_LANES - 1));
@@ -531,11 +568,11 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                 src = a + off * ib;
             }
             if (e == cudaSuccess)
-                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, cfan, w[lane],
+                e = typed_io(kind, src, a + off * ib, b + off * ib, a + off * ib, cn, 0, m, 0, 0, p.cfan, w[lane],
                              cst);
             // the lane's next chunk sort clears the word again: read it now
             if (e == cudaSuccess)
-                e = watch.watch(static_cast<char*>(w[lane]) + typed_scratch_io(kind, cn, 0, cfan, 0) - 256, cst);
+                e = watch.watch(w[lane] + typed_scratch_io(kind, cn, 0, p.cfan, 0) - 256, cst);
         }
         if (e == cudaSuccess) {
             for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(st, event_on(lanes[i]), 0);
@@ -543,37 +580,41 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
                 // one k-way pass into HBM in 16 slices; each finished slice goes
                 // to the host on the copy stream while the next ones merge (at
                 // 1 GiB, 8 slices finish 0.1-0.2 ms later and 32 about 1 ms later)
-                SliceCopy sc_ctx{st, sc, static_cast<const char*>(B), static_cast<char*>(host_out), ib, &evs,
-                                 cudaSuccess};
-                e = typed_kway_final(kind, A, B, n, chunk_n, mfan, m, wm, st, 16, &SliceCopy::on, &sc_ctx);
+                SliceCopy sc_ctx{st, sc, b, static_cast<char*>(host_out), ib, &evs, cudaSuccess};
+                e = typed_kway_final(kind, a, b, n, chunk_n, p.mfan, m, wm, st, 16, &SliceCopy::on, &sc_ctx);
                 if (e == cudaSuccess) e = sc_ctx.e;
-                if (e == cudaSuccess) e = watch.watch(static_cast<char*>(wm) + typed_kway_final_err(kind, n), st);
-                cudaStreamWaitEvent(st, event_on(sc), 0);  // B is freed on st after the copies
+                if (e == cudaSuccess) e = watch.watch(wm + typed_kway_final_err(kind, n), st);
+                cudaStreamWaitEvent(st, event_on(sc), 0);  // the block is free after the copies
             } else {
                 // merges from runs of chunk_n (one pass unless more than 16
                 // chunks form a run); a pass must not write A while the first
-                // one reads it; the last pass writes the host buffer directly
+                // one reads it; the last pass writes the output directly
                 int passes = 0;
-                for (uint64_t r = chunk_n; r < limit; r *= (uint64_t)mfan) ++passes;
-                void* wa = ((passes - 1) & 1) ? B : A;
-                void* wb = ((passes - 1) & 1) ? A : B;
-                e = typed_io(kind, A, vout, wa, wb, n, sort_n, 0, m, chunk_n, mfan, wm, st);
+                for (uint64_t r = chunk_n; r < limit; r *= (uint64_t)p.mfan) ++passes;
+                void* wa = ((passes - 1) & 1) ? (void*)b : (void*)a;
+                void* wb = ((passes - 1) & 1) ? (void*)a : (void*)b;
+                e = typed_io(kind, a, vout, wa, wb, n, sort_n, 0, m, chunk_n, p.mfan, wm, st);
                 if (e == cudaSuccess)
-                    e = watch.watch(static_cast<char*>(wm) + typed_scratch_io(kind, n, sort_n, mfan, chunk_n) - 256, st);
+                    e = watch.watch(wm + typed_scratch_io(kind, n, sort_n, p.mfan, chunk_n) - 256, st);
             }
         }
-        for (cudaEvent_t ev : evs) cudaEventDestroy(ev);  // released once their work completes
     }
-    if (wm) cudaFreeAsync(wm, st);
-    for (void* p : w)
-        if (p) cudaFreeAsync(p, st);
-    if (B) cudaFreeAsync(B, st);
-    cudaFreeAsync(A, st);
     const cudaError_t es = cudaStreamSynchronize(st);
+    for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
     if (e != cudaSuccess) return cuda_fail(e, "host sort");
     if (es != cudaSuccess) return cuda_fail(es, "stream sync");
     if (watch.timed_out()) return fail(ORIGAMI_ERR_TIMEOUT, "a merge kernel's bulk-copy wait expired");
     return ORIGAMI_OK;
+}
+
+int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n,
+                     uint64_t sort_n, unsigned min_k, cudaStream_t st) {
+    const HostPipePlan p = host_pipe_plan(kind, n, sort_n, min_k);
+    void* block = nullptr;
+    CK(cudaMallocAsync(&block, p.total, st), "arena allocation");
+    const int rc = host_pipe_run(kind, host_in, host_out, vin, vout, n, sort_n, p, block, st);
+    cudaFreeAsync(block, st);
+    return rc;
 }
 
 // Table entries of a tuning file: one "kind size_class fan variant" line each.
@@ -644,6 +685,20 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
 }  // namespace
 
 namespace origami {
+uint64_t host_pipe_bytes(int kind, uint64_t n) { return host_pipe_plan(kind, n, 0, 0).total; }
+
+int host_pipe_sort(int kind, const void* in, void* out, uint64_t n, void* block, cudaStream_t st) {
+    auto view = [](const void* p) -> void* {
+        if (is_device_pointer(p)) return const_cast<void*>(p);
+        return device_view(const_cast<void*>(p));
+    };
+    void* vin = view(in);
+    void* vout = view(out);
+    if (!vin || !vout || ((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
+        return fail(ORIGAMI_ERR_INVALID, "buffers the device cannot address directly");
+    return host_pipe_run(kind, const_cast<void*>(in), out, vin, vout, n, 0, host_pipe_plan(kind, n, 0, 0), block, st);
+}
+
 int noalloc_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int noalloc_check(int kind, const void* d, const void* tmp, uint64_t n, uint64_t sort_n,
                   void** result) {

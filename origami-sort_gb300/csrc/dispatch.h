@@ -63,6 +63,16 @@ cudaError_t seg_launch(int kind, void* d, void* tmp, const uint64_t* off, uint64
 // (ORIGAMI_ERR_INVALID), 0 none.
 inline bool err_word_timeout(int w) { return w == 1 || w == 3; }
 
+// capi.cu: the pipelined sort of one array whose buffers the device can
+// address (host memory the GPU reads through its mapping or page tables, or
+// device memory): chunks copied in while earlier chunks sort, then one k-way
+// pass whose output slices leave while later slices merge. host_pipe_bytes is
+// the device memory it needs (one block, caller-owned); host_pipe_sort runs it
+// on `st` and the calling thread's helper streams and returns once the result
+// is in `out` (ORIGAMI_ERR_INVALID when a buffer is not device-addressable).
+uint64_t host_pipe_bytes(int kind, uint64_t n);
+int host_pipe_sort(int kind, const void* in, void* out, uint64_t n, void* block, cudaStream_t st);
+
 // capi.cu: sets the thread's last-error message; makes the stream-ordered pool
 // the caching device arena (returns an ORIGAMI_* status).
 int api_fail(int code, const char* msg);

@@ -411,21 +411,13 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
             diag = (tid - first) * VO;
             cnt = min(VO, la + lb - diag);
         }
-        if constexpr (STABLE) {
-            // serial merge of the block: its end split comes from the next block
-            if (p >= 0) split[tid] = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
-            __syncthreads();
-            if (p >= 0) {
-                const int sa = split[tid];
-                const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
-                merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
-            }
-        } else {
-            // windows from the block's own split: no exchange of splits
-            if (p >= 0) {
-                const int sa = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
-                merge_window_regs<T, VT>(buf, a0, la, b0, lb, sa, diag, r);
-            }
+        // the block's end split comes from the next block's search
+        if (p >= 0) split[tid] = merge_path_ix<T, LinIdx>(buf, a0, la, b0, lb, diag);
+        __syncthreads();
+        if (p >= 0) {
+            const int sa = split[tid];
+            const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
+            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
         }
         // next round's geometry (the other buffer; nothing reads it this round)
         if (tid < npairs) {

@@ -145,35 +145,6 @@ __device__ __forceinline__ void merge_block_regs(const T* src, int ia0, int ib0,
     }
 }
 
-// Keys only: the VT smallest items of the merge of A and B from the split
-// (ia, ib) = (sa, diag - sa) into out[], ascending, with A = src[a0 .. a0+la)
-// and B = src[b0 .. b0+lb). The first VT outputs of that merge lie inside the
-// windows A[sa .. sa+VT) and B[ib .. ib+VT); for sorted windows a and b,
-// min(a[i], b[VT-1-i]) holds exactly the VT smallest of the two as a bitonic
-// sequence, which the half-cleaner network sorts. A window reaching past its
-// list's end reads +inf there. The thread needs only its own split, no end
-// split from a neighbour. Reads at most VT items past the end of B and of A
-// (read slack in the buffer).
-template <class T, int VT, class IX = LinIdx>
-__device__ __forceinline__ void merge_window_regs(const T* src, int a0, int la, int b0, int lb, int sa, int diag,
-                                                  T (&out)[VT]) {
-    const int sb = diag - sa;
-    const int ia = a0 + sa, ib = b0 + sb;
-    if (sa + VT <= la && sb + VT <= lb) {
-#pragma unroll
-        for (int i = 0; i < VT; ++i) out[i] = min(src[IX::at(ia + i)], src[IX::at(ib + VT - 1 - i)]);
-    } else {
-        const T inf = Traits<T>::max_item();
-#pragma unroll
-        for (int i = 0; i < VT; ++i) {
-            const T x = (sa + i < la) ? src[IX::at(ia + i)] : inf;
-            const T y = (sb + VT - 1 - i < lb) ? src[IX::at(ib + VT - 1 - i)] : inf;
-            out[i] = min(x, y);
-        }
-    }
-    bitonic_clean<T, VT>(out);
-}
-
 // Round over pairs of equal width w inside `total` items (the last pair may be
 // short or absent): the tile sort's rounds. `split` is shared scratch of
 // blocks + 1 ints, blocks = ceil(total / VO) + total / (2w) + 1.
@@ -184,33 +155,6 @@ __device__ __forceinline__ void merge_round_uniform(const T* src, T* dst, int w,
     const int bpp = (2 * w + VO - 1) / VO;  // blocks per full pair
     const int npairs = (total + 2 * w - 1) / (2 * w);
     const int nblk = npairs * bpp;
-    if constexpr (!STABLE) {
-        // keys: every block merges the windows at its own split (no split
-        // exchange, one barrier per round)
-        (void)split;
-        for (int blk = tid; blk < nblk; blk += NT) {
-            const int p = blk / bpp;
-            const int a0 = p * 2 * w;
-            const int b0 = min(a0 + w, total), e0 = min(a0 + 2 * w, total);
-            const int diag = (blk - p * bpp) * VO;
-            const int cnt = min(VO, e0 - a0 - diag);
-            if (cnt <= 0) continue;
-            const int sa = merge_path_ix<T, IX>(src, a0, b0 - a0, b0, e0 - b0, diag);
-            T v[VT];
-            merge_window_regs<T, VT, IX>(src, a0, b0 - a0, b0, e0 - b0, sa, diag, v);
-            T* o = dst + a0 + diag;
-            if (cnt == VO) {
-#pragma unroll
-                for (int i = 0; i < VO; ++i) o[i] = v[i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < VO; ++i)
-                    if (i < cnt) o[i] = v[i];
-            }
-        }
-        __syncthreads();
-        return;
-    }
     for (int blk = tid; blk < nblk; blk += NT) {
         const int p = blk / bpp;
         const int a0 = p * 2 * w;
@@ -321,20 +265,15 @@ __device__ __forceinline__ void merge_pair_round_inplace(T* buf, int as, int na,
     const int tid = threadIdx.x;
     const int total = na + nb;
     const int nblk = (total + VO - 1) / VO;
+    if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, as, na, bs, nb, tid * VO);
+    __syncthreads();
     T r[VT];
     const int diag = tid * VO;
     const int cnt = tid < nblk ? min(VO, total - diag) : 0;
-    if constexpr (STABLE) {
-        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, as, na, bs, nb, diag);
-        __syncthreads();
-        if (tid < nblk) {
-            const int sa = split[tid];
-            const int ea = (tid + 1 < nblk) ? split[tid + 1] : na;
-            merge_block_regs<T, VT, STABLE>(buf, as + sa, bs + (diag - sa), ea - sa, cnt, r);
-        }
-    } else if (tid < nblk) {
-        const int sa = merge_path_ix<T, LinIdx>(buf, as, na, bs, nb, diag);
-        merge_window_regs<T, VT>(buf, as, na, bs, nb, sa, diag, r);
+    if (tid < nblk) {
+        const int sa = split[tid];
+        const int ea = (tid + 1 < nblk) ? split[tid + 1] : na;
+        merge_block_regs<T, VT, STABLE>(buf, as + sa, bs + (diag - sa), ea - sa, cnt, r);
     }
     __syncthreads();
     if (cnt == VO) {

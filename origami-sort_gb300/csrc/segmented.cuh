@@ -360,7 +360,7 @@ struct SegPair {
 // kernel: the pair's first item, the tile's output range within the pair, the
 // A run length and four flags in its top bits.
 struct SegTileRec {
-    uint64_t base, d0, d1, la_flags, lb;
+    uint64_t base, d0, d1, la_flags;
     static constexpr uint64_t SRC_TMP = 1ull << 60, DST_TMP = 1ull << 61, LAST = 1ull << 62, PAIR_END = 1ull << 63;
     static constexpr uint64_t LA_MASK = (1ull << 60) - 1;
 };
@@ -391,7 +391,6 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
         r.d0 = p.d0;
         r.d1 = p.d1;
         r.la_flags = f;
-        r.lb = p.lb;
         st.rec[j] = r;
     }
 }
@@ -409,21 +408,18 @@ struct SegBulkGeom {
     uint64_t flags;
 };
 
-// Splits that are inconsistent (runs that are not sorted) are clamped into
-// the runs and reported in *err (ERR_BAD_RUNS).
+// (The runs are always this sort's own tile-sorted or merged output; after an
+// expired wait the merge kernels stop before they read any.)
 template <class T>
 __device__ __forceinline__ SegBulkGeom seg_bulk_issue(T* stage, const T* d, const T* tmp, uint64_t j,
-                                                      const SegTileRec& r, int64_t s0, int64_t s1, uint64_t* bar,
-                                                      int* err) {
+                                                      const SegTileRec& r, int64_t s0, int64_t s1, uint64_t* bar) {
     constexpr int V = Vec<T>::N;
     const uint64_t la = r.la_flags & SegTileRec::LA_MASK;
     const int64_t a1 = (r.la_flags & SegTileRec::PAIR_END) ? (int64_t)la : s1;
     SegBulkGeom q;
     q.job = j;
     q.flags = r.la_flags;
-    bool bad;
-    q.na = tile_split(s0, a1, (int64_t)r.d0, (int)(r.d1 - r.d0), (int64_t)la, (int64_t)r.lb, &bad);
-    if (bad) err_first(err, ERR_BAD_RUNS);
+    q.na = (int)(a1 - s0);
     q.nb = (int)(r.d1 - r.d0) - q.na;
     q.obase = r.base + r.d0;
     q.sh = (int)(q.obase % V);
@@ -472,8 +468,7 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         mbar_init(&bar[1], 1);
         mbar_init_fence();
         const uint64_t j0 = blockIdx.x;
-        geom[0] = seg_bulk_issue<T>(stage(0), d, tmp, j0, st.rec[j0], st.splits[j0], st.splits[j0 + 1], &bar[0],
-                                    st.err);
+        geom[0] = seg_bulk_issue<T>(stage(0), d, tmp, j0, st.rec[j0], st.splits[j0], st.splits[j0 + 1], &bar[0]);
         nj = claim_next();
         if (nj < total) {
             nr = st.rec[nj];
@@ -500,7 +495,7 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         if (tid == 0) {
             if (nj < total) {
                 bulk_wait_read<0>();
-                geom[s ^ 1] = seg_bulk_issue<T>(stage(s ^ 1), d, tmp, nj, nr, n0, n1, &bar[s ^ 1], st.err);
+                geom[s ^ 1] = seg_bulk_issue<T>(stage(s ^ 1), d, tmp, nj, nr, n0, n1, &bar[s ^ 1]);
             } else {
                 geom[s ^ 1].job = total;
             }
@@ -515,21 +510,15 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         T* buf = stage(s);
         const int tot = q.na + q.nb;
         const int nblk = (tot + VO - 1) / VO;
+        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
+        __syncthreads();
         T r[C::P_VT];
         const int diag = tid * VO;
         const int cnt = tid < nblk ? min(VO, tot - diag) : 0;
-        if constexpr (C::STABLE) {
-            if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
-            __syncthreads();
-            if (tid < nblk) {
-                const int sa = split[tid];
-                const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-                merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
-            }
-        } else if (tid < nblk) {
-            // keys: windows at the block's own split (merge_core.cuh)
-            const int sa = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
-            merge_window_regs<T, C::P_VT>(buf, q.as, q.na, q.bs, q.nb, sa, diag, r);
+        if (tid < nblk) {
+            const int sa = split[tid];
+            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
         }
         __syncthreads();
         // stage index x holds output item x - sh, so x = 0 lies on a 16-byte

@@ -465,21 +465,15 @@ __global__ void __launch_bounds__(NT, MINB)
         // one merge round, outputs kept in registers until every thread has
         // read its inputs, then written back over the stage
         const int nblk = (total + VO - 1) / VO;
+        if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
+        __syncthreads();
         T r[VT];
         const int diag = tid * VO;
         const int cnt = tid < nblk ? min(VO, total - diag) : 0;
-        if constexpr (STABLE) {
-            if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
-            __syncthreads();
-            if (tid < nblk) {
-                const int sa = split[tid];
-                const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-                merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
-            }
-        } else if (tid < nblk) {
-            // keys: windows at the block's own split (merge_core.cuh)
-            const int sa = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, diag);
-            merge_window_regs<T, VT>(buf, q.as, q.na, q.bs, q.nb, sa, diag, r);
+        if (tid < nblk) {
+            const int sa = split[tid];
+            const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
+            merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
         }
         __syncthreads();
         if (cnt == VO) {

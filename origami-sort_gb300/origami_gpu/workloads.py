@@ -305,6 +305,31 @@ def serving(torch, rates=(100, 200, 400, 800), duration_s=3.0, pool_size=96, see
         check(L.origami_sort(it["kind"], it["out"].data_ptr(), None, it["n"], 0, 0, 0, ctypes.byref(res)))
         dt += time.perf_counter() - t0
     out["loop_plain_keys_per_s"] = pool.keys / dt
+    if out.get("saturation", {}).get("keys_per_s"):
+        out["saturation_vs_loop_plain"] = out["saturation"]["keys_per_s"] / out["loop_plain_keys_per_s"]
+    # the host link: what the largest request's copies cost at the least
+    big = max(pool.items, key=lambda it: it["in"].numel())
+    nbytes = big["in"].numel() * 4
+    dev_buf = torch.empty(big["in"].numel(), dtype=torch.int32, device=dev or "cuda")
+    ts_in, ts_out = [], []
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        c = torch.cuda.Event(enable_timing=True)
+        a.record()
+        dev_buf.copy_(big["in"], non_blocking=True)
+        b.record()
+        big["out"].copy_(dev_buf, non_blocking=True)
+        c.record()
+        torch.cuda.synchronize()
+        ts_in.append(a.elapsed_time(b))
+        ts_out.append(b.elapsed_time(c))
+    del dev_buf
+    out["largest_request"] = {"kind": big["kind"], "n": big["n"], "bytes": nbytes,
+                              "copy_in_ms": min(ts_in), "copy_out_ms": min(ts_out),
+                              "host_link_in_gbs": nbytes / min(ts_in) / 1e6,
+                              "host_link_out_gbs": nbytes / min(ts_out) / 1e6,
+                              "link_floor_ms": min(ts_in) + min(ts_out)}
     return out
 
 

@@ -197,3 +197,28 @@ def test_wait_timeout_then_result():
         if not done:
             s.wait(rid)
     assert np.array_equal(x, expected(a))
+
+
+def test_large_requests_take_the_pipelined_sort():
+    # requests of 2^22 items and more run on the server's helper threads as the
+    # pipelined single-array sort (copies overlapping the sort), beside
+    # segmented batches of small ones; every result equals the stable sort
+    rng = np.random.default_rng(21)
+    specs = [(og.U32, (1 << 24) + 333, True), (og.KVU64, 1 << 22, False), (og.U64, 3 * (1 << 22) + 5, True),
+             (og.U32, 5000, False), (og.KVU64, 70_000, True), (og.U32, 1 << 22, False)]
+    inputs = [make(k, n, rng, zipf=(i % 2 == 0), pinned=p) for i, (k, n, p) in enumerate(specs)]
+    outs = [og.empty_host(k, n, pinned=p) for (k, n, p) in specs]
+    dev_in = torch.from_numpy(make(og.U64, 1 << 23, rng).view(np.uint8).copy()).cuda()
+    dev_keep = dev_in.clone()
+    with og.Server() as s:
+        ids = [s.submit(a, out=o) for a, o in zip(inputs, outs)]
+        ids.append(s.submit(dev_in, kind=og.U64))
+        for r in ids:
+            s.wait(r)
+        st = s.stats()
+    assert st["completed"] == len(ids) and st["failed"] == 0
+    for a, o in zip(inputs, outs):
+        assert np.array_equal(o, expected(a))
+    torch.cuda.synchronize()
+    got = dev_in.cpu().numpy().view(np.uint64)
+    assert np.array_equal(got, np.sort(dev_keep.cpu().numpy().view(np.uint64)))
