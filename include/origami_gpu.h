@@ -242,19 +242,28 @@ int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_t n, uint64
 
 /*
  * Serving loop (no counterpart in the reference, whose callers sort one array
- * per call). A server owns one worker thread that runs continuous batching:
+ * per call). A server owns one worker thread that runs continuous batching and
+ * two helper threads:
  *   - submit() queues a request: sort the `n` items of `kind` at `in` into
  *     `out` (out == in or NULL: in place; otherwise the two must not overlap).
  *     Each may be host pageable, host pinned or device memory, with any
  *     alignment; n = 0 completes at once. Both buffers must stay valid, and
  *     `out` untouched, until wait() returns for the request.
- *   - Requests are admitted in arrival order while the HBM budget allows (a
- *     batch reserves twice its items, its offsets and the segmented sort's
- *     scratch) and fewer than max_inflight batches are on the GPU. The oldest
- *     request that does not fit waits for running batches to return memory.
- *   - Admitted requests of one kind are coalesced into one batched segmented
- *     sort (at most max_batch_items items unless one request is larger). Each
- *     batch runs on its own stream, so new batches overlap running ones.
+ *   - Requests are admitted in arrival order while the HBM budget allows and
+ *     fewer than max_inflight batches are on the GPU. The oldest request that
+ *     does not fit waits for running batches to return memory.
+ *   - Device memory comes from the server's arena: slabs held until the server
+ *     is destroyed, carved into blocks per batch; after warm-up no request
+ *     allocates device memory.
+ *   - A request of 2^24 items or more whose buffers the device can address
+ *     (pinned or device memory; pageable memory on hosts whose GPU reads the
+ *     host's page tables), 16-byte aligned, is a batch of its own: a helper
+ *     thread runs the pipelined single-array sort on it (its chunks copied in
+ *     while earlier chunks sort, its output copied out while later slices
+ *     merge). Smaller requests of one kind are coalesced into one batched
+ *     segmented sort (at most max_batch_items items unless one request is
+ *     larger), each batch on its own stream, so new batches overlap running
+ *     ones; pageable outputs are copied out by a helper thread.
  *   - Results are identical to sorting each request alone (key-value requests
  *     stably).
  * Errors: ORIGAMI_ERR_OOM at submit for a request that can never fit the
@@ -264,10 +273,10 @@ int origami_sort_noalloc_device(int kind, void* d, void* tmp, uint64_t n, uint64
  * from wait() for a cancelled request; a failed batch's status (OOM when the
  * device could not supply the budgeted memory) from wait() for each of its
  * requests. wait() collects a finished request: its id is unknown afterwards.
- * Zero arguments to create() select the defaults: 120 GiB budget, 4 batches in
+ * Zero arguments to create() select the defaults: 120 GiB budget, 6 batches in
  * flight, 2^28 items per batch, 2^20 pending requests. destroy() cancels what
- * is pending, waits for the batches in flight and frees the server; no other
- * call on it may be in progress.
+ * is pending, waits for the batches in flight and frees the server and its
+ * arena; no other call on it may be in progress.
  */
 typedef struct origami_server origami_server;
 
@@ -280,6 +289,8 @@ typedef struct origami_server_stats {
     uint64_t max_concurrent_batches;                  /* most batches in flight at once */
     double p50_ms, p99_ms, max_ms;                    /* latency, submission to completion */
     double keys_per_s; /* keys / (last completion - first submission) */
+    uint64_t pipe_batches;              /* large requests run as the pipelined sort (in batches) */
+    uint64_t arena_bytes, arena_grows;  /* the server's device arena: bytes held, slab allocations */
 } origami_server_stats;
 
 int origami_serve_create(origami_server** out, uint64_t hbm_budget_bytes, int max_inflight,

@@ -180,16 +180,18 @@ struct KbCuts {
     int* run;
 };
 
-// One CTA per range (blockIdx.x = g * rpg + b): writes the range's cut table.
-// bnd0 (rpg > 1): kway_split_kernel's super-sample counts per range boundary,
-// [g * (rpg+1) + b][KWAY_MAX]. The first CTA resets the merge kernel's tile
+// One CTA per range (blockIdx.x = g * rpg + b): writes the range's cut table,
+// and appends its tiles (as slots r * TPR + c) to the pass's tile list
+// tiles[0 .. *ntiles) (*ntiles is 0 at launch). bnd0 (rpg > 1):
+// kway_split_kernel's super-sample counts per range boundary,
+// [g * (rpg+1) + b][KWAY_MAX]. The first CTA resets the merge kernel's claim
 // counter.
 template <class T>
 __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits<T>::Key* __restrict__ samp,
                                                           uint64_t n, uint64_t run, int fan, int rpg,
                                                           const int64_t* __restrict__ bnd0, KbCuts cuts,
-                                                          uint32_t* __restrict__ ntiles, unsigned* __restrict__ claim,
-                                                          int* __restrict__ err) {
+                                                          uint32_t* __restrict__ tiles, unsigned* __restrict__ ntiles,
+                                                          unsigned* __restrict__ claim, int* __restrict__ err) {
     using Sh = KbShape<T>;
     using K = typename Sh::K;
     using E = typename Sh::E;
@@ -205,6 +207,7 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits
     __shared__ K cy[2];                   // keys of the start / end cut items
     __shared__ int cj[2];                 // their runs (-1: group start / group end)
     __shared__ int cnt_all;
+    __shared__ unsigned tbase;
     const int tid = threadIdx.x;
     const uint64_t bid = blockIdx.x;
     const uint64_t g = bid / (uint64_t)rpg;
@@ -212,10 +215,7 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits
     const KbGroup grp(g, n, run, fan);
     if (bid == 0 && tid == 0) *claim = 0;
     // a wait of an earlier kernel expired: the runs are not sorted, no tiles
-    if (__syncthreads_or(tid == 0 && err_wait_set(err))) {
-        if (tid == 0) ntiles[bid] = 0;
-        return;
-    }
+    if (__syncthreads_or(tid == 0 && err_wait_set(err))) return;
     if (tid < KWAY_MAX) rns[tid] = (tid < fan ? grp.len(tid) : 0) / S;
     __syncthreads();
     const uint64_t sbase = grp.base / S;  // group's first sample (runs start at multiples of S)
@@ -322,9 +322,10 @@ __global__ void __launch_bounds__(KB_CUT_NT) kb_cut_kernel(const typename Traits
     const bool last_range = (b == rpg - 1);
     const int nfull = cnt / M;
     const int nt = nfull + ((last_range || cnt % M) ? 1 : 0);  // tiles of this range
-    if (tid == 0) ntiles[bid] = (uint32_t)nt;
+    if (tid == 0) tbase = atomicAdd(ntiles, (unsigned)nt);
     for (int q = tid; q < (nt + 1) * KWAY_MAX; q += NT) hist[q] = 0;
     __syncthreads();
+    for (int c = tid; c < nt; c += NT) tiles[tbase + c] = (uint32_t)(bid * TPR + (uint64_t)c);
     for (int x = tid; x < cnt; x += NT) atomicAdd(&hist[(x / M) * KWAY_MAX + (merged[x].tag & 15)], 1u);
     __syncthreads();
     // inclusive prefix over tiles: hist[t][k] = run-k samples at merged positions <= end of tile t
@@ -417,7 +418,7 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
         if (p >= 0) {
             const int sa = split[tid];
             const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
-            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
+            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r, a0 + la, b0 + lb);
         }
         // next round's geometry (the other buffer; nothing reads it this round)
         if (tid < npairs) {
@@ -448,7 +449,7 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
 
 // A tile staged in shared memory (written by warp 0).
 struct KbTileGeom {
-    uint64_t slot;  // >= nslots: none (the CTA is done)
+    uint64_t slot;  // ~0: none (the CTA is done)
     uint64_t g;     // its group
     uint64_t o;     // first output item (after the boundary search)
     int total;      // items (after the boundary search)
@@ -462,20 +463,21 @@ struct KbSlice {
     int dq;      // samples of the run in the tile: its end block starts at dq * S
 };
 
-// Persistent merge of every tile of the pass. Tiles are slots
-// [range * TPR + c]; a slot is a tile when c < ntiles[range]. A CTA starts
-// with slot blockIdx.x and claims later ones from *claim (reset by the cut
-// kernel), skipping slots that are no tile. Warp 0 stages the tiles: lane k
-// handles run k (its cut counts fetched one tile ahead), lane 0 the claims and
-// the barrier; once a tile has landed it finds the exact slice of each run by
-// one search in the block at each end. samp_out / ssamp_out (may be null):
-// samples of the output for the next pass.
+// Persistent merge of every tile of the pass: tiles[0 .. *ntiles) (slots
+// range * TPR + c, listed by the cut kernels). A CTA starts with tile
+// blockIdx.x and claims later ones from *claim (reset by the cut kernel).
+// Warp 0 stages the tiles: lane k handles run k, lane 0 the claims and the
+// barrier; once a tile has landed it finds the exact slice of each run by one
+// search in the block at each end. ntiles_next (may be null): the next pass's
+// tile counter, reset here. samp_out / ssamp_out (may be null): samples of the
+// output for the next pass.
 template <class T>
 __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
     kb_merge_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, uint64_t run, int fan, int rpg,
-                    KbCuts cuts, const uint32_t* __restrict__ ntiles, uint64_t nslots, uint64_t xout,
-                    typename Traits<T>::Key* __restrict__ samp_out, typename Traits<T>::Key* __restrict__ ssamp_out,
-                    unsigned* __restrict__ claim, int* err, uint32_t spin) {
+                    KbCuts cuts, const uint32_t* __restrict__ tiles, const unsigned* __restrict__ ntiles,
+                    unsigned* __restrict__ ntiles_next, uint64_t xout, typename Traits<T>::Key* __restrict__ samp_out,
+                    typename Traits<T>::Key* __restrict__ ssamp_out, unsigned* __restrict__ claim, int* err,
+                    uint32_t spin) {
     using Sh = KbShape<T>;
     using C = KbCfg<T>;
     using K = typename Sh::K;
@@ -492,21 +494,23 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
     const uint64_t G = gridDim.x;
     const K* ckey = static_cast<const K*>(cuts.key);
     auto stage = [&](int s) { return reinterpret_cast<T*>(smem_raw + (size_t)s * Sh::STAGE); };
-    // warp 0 lane 0: the next slot that is a tile, from `t` on, claiming more
-    auto next_tile = [&](uint64_t t) -> uint64_t {
-        while (t < nslots && (uint32_t)(t % TPR) >= ntiles[t / TPR]) t = G + (uint64_t)atomicAdd(claim, 1u);
-        return t;
-    };
-    // warp 0 state: the slot staged next, lane k's sample counts of run k at
-    // its two cuts, and the cut items
-    uint64_t nslot = nslots;
+    // Warp 0 runs a three-step look-ahead over the pass's tile list, one step
+    // per tile merged, so that no global load it makes is waited for:
+    //   claim  a tile index (lane 0's atomic)       (cpend)
+    //   load   its slot from the tile list        (mid, mslot)
+    //   load   its cuts: lane k's sample counts of run k, the cut items (nslot, ...)
+    // and the tile with loaded cuts is staged next.
+    const uint64_t NTL = *ntiles;  // tiles of the pass (the cut kernels have finished)
+    uint64_t cpend = NTL, mid = NTL;
+    uint32_t mslot = 0;
+    uint64_t nslot = ~0ull;  // slot staged next (~0: none)
     uint32_t qa = 0, qe = 0;
     K ya = 0, ye = 0;
     int ja = -1, je = -2;
-    auto fetch = [&](uint64_t t) {  // warp 0, uniform t
-        nslot = t;
-        if (t < nslots) {
-            const uint64_t row = (t / TPR) * (uint64_t)(TPR + 1) + t % TPR;  // cut c of the range
+    auto fetch = [&]() {  // the cuts of tile `mid` (its slot loaded last step)
+        nslot = mid < NTL ? (uint64_t)mslot : ~0ull;
+        if (mid < NTL) {
+            const uint64_t row = (nslot / TPR) * (uint64_t)(TPR + 1) + nslot % TPR;  // cut c of the range
             if (lane < KWAY_MAX) {
                 qa = cuts.q[row * KWAY_MAX + lane];
                 qe = cuts.q[(row + 1) * KWAY_MAX + lane];
@@ -517,11 +521,17 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
             je = cuts.run[row + 1];
         }
     };
+    auto step = [&]() {  // warp 0: advance the look-ahead by one tile
+        fetch();
+        mid = __shfl_sync(0xFFFFFFFFu, cpend, 0);  // the claim made one step ago
+        if (mid < NTL) mslot = tiles[mid];
+        if (lane == 0) cpend = mid < NTL ? G + (uint64_t)atomicAdd(claim, 1u) : NTL;
+    };
     // warp 0: stage the fetched tile into stage s (barrier bar[s]): for run k
     // the items from the block of cut c (its start, or the run's start at a
     // group start) to the end of the block of cut c+1 (or the run's end)
     auto issue = [&](int s) {
-        const bool any = nslot < nslots;
+        const bool any = nslot != ~0ull;
         const uint64_t g = nslot / TPR / (uint64_t)rpg;
         const bool mine = lane < fan && any;
         const uint64_t rs = g * run * (uint64_t)fan + (uint64_t)lane * run;  // run start
@@ -560,7 +570,7 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
             sl[s][lane] = v;
         }
         if (lane == 0) {
-            tg[s].slot = any ? nslot : nslots;
+            tg[s].slot = nslot;
             tg[s].g = g;
             cutk[s][0] = ya;
             cutk[s][1] = ye;
@@ -620,37 +630,36 @@ __global__ void __launch_bounds__(KbCfg<T>::NT, KbCfg<T>::MINB)
         mbar_init(&bar[1], 1);
         mbar_init_fence();
     }
+    // the next pass's cut kernel counts its tiles here
+    if (blockIdx.x == 0 && tid == 0 && ntiles_next) *ntiles_next = 0;
     // a wait of an earlier kernel expired: the runs are not sorted, stop here
     if (__syncthreads_or(tid == 0 && err_wait_set(err))) return;
+    if (blockIdx.x >= NTL) return;
     if (tid < 32) {
-        uint64_t t = 0;
-        if (lane == 0) t = next_tile(blockIdx.x < nslots ? (uint64_t)blockIdx.x : nslots);
-        t = __shfl_sync(0xFFFFFFFFu, t, 0);
-        fetch(t);
+        // prime the look-ahead: this CTA's first tile is tile blockIdx.x
+        mid = blockIdx.x;
+        mslot = tiles[mid];
+        if (lane == 0) cpend = G + (uint64_t)atomicAdd(claim, 1u);
+        step();  // cuts of the first tile; slot of the second
         issue(0);
-        if (lane == 0) t = nslot < nslots ? next_tile(G + (uint64_t)atomicAdd(claim, 1u)) : nslots;
-        t = __shfl_sync(0xFFFFFFFFu, t, 0);
-        fetch(t);
+        step();  // cuts of the second tile; slot of the third
     }
     __syncthreads();
     uint32_t phase = 0;  // bit s: parity of stage s's next completion
     for (int s = 0;; s ^= 1) {
-        if (tg[s].slot >= nslots) break;
+        if (tg[s].slot == ~0ull) break;
         // warp 0 stages the next tile into the other stage (its previous bulk
-        // store has left shared memory), then fetches the one after
+        // store has left shared memory), then advances the look-ahead
         if (tid < 32) {
             if (lane == 0) bulk_wait_read<0>();
             __syncwarp();
             issue(s ^ 1);
-            uint64_t t = 0;
-            if (lane == 0) t = nslot < nslots ? next_tile(G + (uint64_t)atomicAdd(claim, 1u)) : nslots;
-            t = __shfl_sync(0xFFFFFFFFu, t, 0);
-            fetch(t);
+            step();
         }
         const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u, spin);
         if (__syncthreads_or(!ok)) {
             if (tid == 0)
-                bulk_drain<2>(err, bar, (1u << s) | (tg[s ^ 1].slot < nslots ? 1u << (s ^ 1) : 0u), phase);
+                bulk_drain<2>(err, bar, (1u << s) | (tg[s ^ 1].slot != ~0ull ? 1u << (s ^ 1) : 0u), phase);
             return;
         }
         phase ^= 1u << s;

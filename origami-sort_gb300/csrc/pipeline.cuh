@@ -244,10 +244,11 @@ inline uint64_t chunk_limit(uint64_t n, uint64_t sort_n) {
 //   k-way passes (only when the plan has some, kway_bulk.cuh):
 //   bnd0       super-sample splits of the range boundaries, [groups][rpg+1][16]
 //   cut q/key/run  the ranges' tile cuts (KbCuts), [ranges][TPR+1]([16])
-//   ntiles     tiles per range
+//   tiles      the pass's tile list (slots), ranges * TPR
 //   samp 0/1   samples (one key per S items) of the runs a pass reads / writes
 //   ssamp 0/1  super-samples (one key per S*64 items)
-//   tail       256 bytes: the error word, then the merge kernels' tile counter
+//   tail       256 bytes: the error word, the merge kernels' claim counter
+//              (+64), the k-way passes' two tile counters (+128, +132)
 template <class T>
 struct PipeScratch {
     using K = typename Traits<T>::Key;
@@ -255,7 +256,8 @@ struct PipeScratch {
     int64_t* splits = nullptr;
     int64_t* bnd0 = nullptr;
     KbCuts cuts{nullptr, nullptr, nullptr};
-    uint32_t* ntiles = nullptr;
+    uint32_t* tiles = nullptr;
+    unsigned* tcount = nullptr;  // [2]: pass p counts its tiles in tcount[p & 1]
     K* samp[2] = {nullptr, nullptr};
     K* ssamp[2] = {nullptr, nullptr};
     int* err = nullptr;
@@ -284,12 +286,13 @@ struct PipeScratch {
             cuts.q = reinterpret_cast<uint32_t*>(take(rows * KWAY_MAX * 4));
             cuts.key = take(rows * sizeof(K));
             cuts.run = reinterpret_cast<int*>(take(rows * 4));
-            ntiles = reinterpret_cast<uint32_t*>(take(rng * 4));
+            tiles = reinterpret_cast<uint32_t*>(take(rows * 4));
             for (int i = 0; i < 2; ++i) samp[i] = reinterpret_cast<K*>(take((n / S + 1) * sizeof(K)));
             for (int i = 0; i < 2; ++i) ssamp[i] = reinterpret_cast<K*>(take((n / (S * KB_SS) + 1) * sizeof(K)));
         }
         err = reinterpret_cast<int*>(take(256));
         claim = b ? reinterpret_cast<unsigned*>(reinterpret_cast<char*>(err) + 64) : nullptr;
+        tcount = b ? reinterpret_cast<unsigned*>(reinterpret_cast<char*>(err) + 128) : nullptr;
         bytes = o;
     }
 };
@@ -469,16 +472,20 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                 if (stats) stats->kernels++;
             }
             const uint64_t ranges = p.groups * (uint64_t)p.rpg;
+            // pass pi lists its tiles in tcount[pi & 1]; the first k-way pass's
+            // counter starts at 0 here, each merge kernel zeroes the next one
+            unsigned* tc = sc.tcount + (pi & 1);
+            if (pi == 0) cudaMemsetAsync(tc, 0, sizeof(unsigned), st);
             launch(n_kc.c_str(), st, [&] {
                 kb_cut_kernel<T><<<(unsigned)ranges, KB_CUT_NT, KbShape<T>::CUT_SMEM, st>>>(
-                    s_in, n, p.run, p.fan, p.rpg, sc.bnd0, sc.cuts, sc.ntiles, claim, err);
+                    s_in, n, p.run, p.fan, p.rpg, sc.bnd0, sc.cuts, sc.tiles, tc, claim, err);
             });
             const uint64_t nslots = ranges * (uint64_t)KbShape<T>::TPR;
             const uint64_t grid = std::min<uint64_t>(nslots, kb_resident<T>());
             launch(n_km.c_str(), st, [&] {
                 kb_merge_kernel<T><<<(unsigned)grid, KbCfg<T>::NT, KbShape<T>::SMEM, st>>>(
-                    cur, nxt, n, p.run, p.fan, p.rpg, sc.cuts, sc.ntiles, nslots, xo, s_out, ss_out, claim, err,
-                    wait_limit());
+                    cur, nxt, n, p.run, p.fan, p.rpg, sc.cuts, sc.tiles, tc, more ? sc.tcount + ((pi + 1) & 1) : nullptr,
+                    xo, s_out, ss_out, claim, err, wait_limit());
             });
             if (stats) stats->kernels += 2;
         }

@@ -518,7 +518,8 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         if (tid < nblk) {
             const int sa = split[tid];
             const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
+            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r,
+                                                    q.as + q.na, q.bs + q.nb);
         }
         __syncthreads();
         // stage index x holds output item x - sh, so x = 0 lies on a 16-byte

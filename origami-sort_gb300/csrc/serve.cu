@@ -66,8 +66,11 @@ struct Request {
 
 // Largest size ratio between requests of one batch (the first and each other).
 constexpr uint64_t SIZE_RATIO = 64;
-// Requests of at least this many items take the pipelined single-array sort.
-constexpr uint64_t PIPE_MIN = 1ull << 22;
+// Requests of at least this many items take the pipelined single-array sort:
+// from 2^24 items on it runs chunked, its copies on the copy engines (smaller
+// sorts of host buffers would read and write the host inside their kernels,
+// holding the SMs for the whole transfer while other batches wait).
+constexpr uint64_t PIPE_MIN = 1ull << 24;
 constexpr int HELPERS = 2;
 
 // The server's device arena: slabs of device memory kept until the server is
@@ -81,7 +84,8 @@ class Arena {
     };
     std::vector<Slab> slabs_;
     std::map<char*, uint64_t> free_;  // free ranges: start -> bytes
-    uint64_t reserved_ = 0;
+    uint64_t reserved_ = 0, grows_ = 0;
+    cudaStream_t st_ = nullptr;  // slab allocations (stream-ordered: no device-wide synchronization)
 
     const Slab* slab_of(const char* p) const {
         for (const Slab& s : slabs_)
@@ -90,27 +94,35 @@ class Arena {
     }
 
   public:
-    ~Arena() { trim(true); }
+    ~Arena() {
+        trim(true);
+        if (st_) cudaStreamDestroy(st_);
+    }
     uint64_t reserved() const { return reserved_; }
-    // A block of `bytes`, growing by a new slab (at least `slab_min` bytes)
-    // while the slabs stay within `cap` bytes; nullptr when neither works.
+    uint64_t grows() const { return grows_; }
+    // A block of `bytes`, growing by a new slab (at least `slab_min` bytes, and
+    // half of what is reserved, so that growth is rare) while the slabs stay
+    // within `cap` bytes; nullptr when neither works.
     char* alloc(uint64_t bytes, uint64_t cap, uint64_t slab_min) {
         bytes = (bytes + 255) & ~255ull;
         auto best = free_.end();
         for (auto it = free_.begin(); it != free_.end(); ++it)
             if (it->second >= bytes && (best == free_.end() || it->second < best->second)) best = it;
         if (best == free_.end()) {
-            uint64_t sz = std::max(bytes, slab_min);
+            uint64_t sz = std::max(std::max(bytes, slab_min), reserved_ / 2);
             sz = (sz + (2ull << 20) - 1) & ~((2ull << 20) - 1);
             if (reserved_ + sz > cap) sz = bytes;
             if (reserved_ + sz > cap) return nullptr;
+            if (!st_) cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
             char* p = nullptr;
-            if (cudaMalloc(reinterpret_cast<void**>(&p), sz) != cudaSuccess) {
+            if (cudaMallocAsync(reinterpret_cast<void**>(&p), sz, st_) != cudaSuccess ||
+                cudaStreamSynchronize(st_) != cudaSuccess) {
                 cudaGetLastError();
                 return nullptr;
             }
             slabs_.push_back({p, sz});
             reserved_ += sz;
+            ++grows_;
             best = free_.emplace(p, sz).first;
         }
         char* p = best->first;
@@ -143,7 +155,7 @@ class Arena {
             const bool empty = it != free_.end() && it->second == slabs_[i].size;
             if (empty || all) {
                 if (it != free_.end()) free_.erase(it);
-                cudaFree(slabs_[i].base);
+                cudaFreeAsync(slabs_[i].base, st_);
                 reserved_ -= slabs_[i].size;
                 slabs_.erase(slabs_.begin() + (long)i);
             } else {
@@ -151,6 +163,7 @@ class Arena {
             }
         }
         if (all) free_.clear();
+        if (st_) cudaStreamSynchronize(st_);
     }
 };
 
@@ -238,6 +251,7 @@ struct origami_server {
     std::vector<int*> err_words;
     std::vector<std::unique_ptr<Batch>> abandoned;  // kept: a late marker may still touch them
     Arena arena;  // used by the worker thread only
+    std::atomic<uint64_t> arena_reserved{0}, arena_grows{0};  // its figures, for get_stats
     std::thread worker;
 
     // helper threads: large requests and pageable copies (tasks under mu)
@@ -405,6 +419,8 @@ struct origami_server {
     // cannot supply it now.
     bool take_block(Batch& b) {
         b.block = arena.alloc(b.bytes, budget, std::min<uint64_t>(budget, 1ull << 30));
+        arena_reserved.store(arena.reserved());
+        arena_grows.store(arena.grows());
         return b.block != nullptr;
     }
 
@@ -766,6 +782,9 @@ int origami_serve_get_stats(origami_server* s, origami_server_stats* out) {
     out->max_ms = l.empty() ? 0.0 : l.back();
     const double sec = s->have_first ? std::chrono::duration<double>(s->t_last - s->t_first).count() : 0.0;
     out->keys_per_s = sec > 0 ? (double)s->keys / sec : 0.0;
+    out->pipe_batches = s->pipe_batches;
+    out->arena_bytes = s->arena_reserved.load();
+    out->arena_grows = s->arena_grows.load();
     return ORIGAMI_OK;
 }
 
@@ -773,7 +792,7 @@ int origami_serve_reset_stats(origami_server* s) {
     if (!s) return origami::api_fail(ORIGAMI_ERR_INVALID, "server is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat_ms.clear();
-    s->submitted = s->completed = s->failed = s->cancelled = s->keys = s->batches = 0;
+    s->submitted = s->completed = s->failed = s->cancelled = s->keys = s->batches = s->pipe_batches = 0;
     s->max_concurrent = s->inflight.size();
     s->peak_in_use = s->in_use;
     s->have_first = false;

@@ -45,7 +45,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_uint64) for f in (
         "submitted", "completed", "failed", "cancelled", "keys", "batches", "pending",
         "bytes_reserved", "peak_bytes_reserved", "max_concurrent_batches")] + \
-        [(f, ctypes.c_double) for f in ("p50_ms", "p99_ms", "max_ms", "keys_per_s")]
+        [(f, ctypes.c_double) for f in ("p50_ms", "p99_ms", "max_ms", "keys_per_s")] + \
+        [(f, ctypes.c_uint64) for f in ("pipe_batches", "arena_bytes", "arena_grows")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -271,9 +271,9 @@ def serving(torch, rates=(100, 200, 400, 800), duration_s=3.0, pool_size=96, see
                        f"{pool_size} distinct pinned-host requests reused round robin "
                        f"({pool.bytes / 2**30:.1f} GiB); HBM budget {budget >> 30} GiB",
            "rates": []}
-    fields = ("offered_rate", "requests", "completed", "failed", "keys", "batches",
-              "max_concurrent_batches", "peak_bytes_reserved", "p50_ms", "p99_ms", "max_ms",
-              "keys_per_s")
+    fields = ("offered_rate", "requests", "completed", "failed", "keys", "batches", "pipe_batches",
+              "max_concurrent_batches", "peak_bytes_reserved", "arena_bytes", "arena_grows", "p50_ms", "p99_ms",
+              "max_ms", "keys_per_s")
     with Server(hbm_budget_bytes=budget) as s:
         # warm-up: every request once (arena growth, first touch of host pages)
         serve_rate(s, pool, None, 0, seed, max_requests=len(pool.items))

@@ -200,11 +200,11 @@ def test_wait_timeout_then_result():
 
 
 def test_large_requests_take_the_pipelined_sort():
-    # requests of 2^22 items and more run on the server's helper threads as the
+    # requests of 2^24 items and more run on the server's helper threads as the
     # pipelined single-array sort (copies overlapping the sort), beside
-    # segmented batches of small ones; every result equals the stable sort
+    # segmented batches of smaller ones; every result equals the stable sort
     rng = np.random.default_rng(21)
-    specs = [(og.U32, (1 << 24) + 333, True), (og.KVU64, 1 << 22, False), (og.U64, 3 * (1 << 22) + 5, True),
+    specs = [(og.U32, (1 << 24) + 333, True), (og.KVU64, 1 << 22, False), (og.U64, (1 << 24) + 5, False),
              (og.U32, 5000, False), (og.KVU64, 70_000, True), (og.U32, 1 << 22, False)]
     inputs = [make(k, n, rng, zipf=(i % 2 == 0), pinned=p) for i, (k, n, p) in enumerate(specs)]
     outs = [og.empty_host(k, n, pinned=p) for (k, n, p) in specs]
@@ -217,6 +217,7 @@ def test_large_requests_take_the_pipelined_sort():
             s.wait(r)
         st = s.stats()
     assert st["completed"] == len(ids) and st["failed"] == 0
+    assert st["pipe_batches"] >= 2 and st["arena_bytes"] > 0
     for a, o in zip(inputs, outs):
         assert np.array_equal(o, expected(a))
     torch.cuda.synchronize()
