@@ -341,6 +341,25 @@ int origami_tuning_set(int kind, uint64_t n, int fan, int variant);
 int origami_tuning_save(const char* path);
 int origami_tuning_load(const char* path);
 
+/*
+ * Segmented-sort tuning (no counterpart in the reference; its analogue is the
+ * compile-time config.h tables and the bench_sort_phases sweeps). The level
+ * merges of a batched segmented sort use one of two merge shapes: 0 (the
+ * default) is the binary pass's first tile shape, 1 its second (twice the tile,
+ * more threads). The table is keyed by item kind and the size class
+ * floor(log2(n / nseg)) of the mean segment length; every segmented launch
+ * (origami_sort_segmented*, origami_seg_plan_create, the serving loop's
+ * batches) takes its shape from it.
+ *   origami_autotune_segmented  times both shapes on the caller's own device
+ *                      segments (d is left holding its input), stores the
+ *                      faster; `report` (may be NULL) gets "shape= ms=" lines.
+ *   get / set          read or write one entry (shape 0 or 1).
+ */
+int origami_autotune_segmented(int kind, void* d, void* tmp, const uint64_t* offsets, uint64_t nseg, uint64_t n,
+                               char* report, uint64_t cap);
+int origami_seg_tuning_get(int kind, uint64_t n, uint64_t nseg, int* shape);
+int origami_seg_tuning_set(int kind, uint64_t n, uint64_t nseg, int shape);
+
 /* Device arena used by the host-pointer calls and by the serving loop. */
 int origami_arena_reserve(uint64_t bytes);  /* pre-grow the pool */
 int origami_arena_trim(void);               /* return cached memory to the driver */

@@ -262,6 +262,17 @@ int shape_for(int kind, uint64_t n, unsigned min_k) {
     return shape_code(fan_of(min_k), 0);
 }
 
+// Segmented sorts: the level merges' merge shape (0 / 1, SegMergeCfg) per
+// kind and size class of the mean segment length. Default 0.
+std::atomic<int> g_seg_tune[5][TUNE_CLASSES];
+
+int seg_class(uint64_t n, uint64_t nseg) { return size_class(nseg ? n / nseg : n); }
+
+int seg_shape_for(int kind, uint64_t n, uint64_t nseg) {
+    std::call_once(g_tune_once, tune_init);
+    return g_seg_tune[kind][seg_class(n, nseg)].load(std::memory_order_relaxed);
+}
+
 cudaError_t run_typed(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, void* want,
                       int fan, void* scratch, cudaStream_t st) {
     const uint64_t m = key_mask(kind);
@@ -636,6 +647,8 @@ int tune_load_file(const char* path) {
 void tune_init() {
     for (auto& row : g_tune)
         for (auto& c : row) c.store(shape_code(2, 0), std::memory_order_relaxed);
+    for (auto& row : g_seg_tune)
+        for (auto& c : row) c.store(0, std::memory_order_relaxed);
     if (const char* path = std::getenv("ORIGAMI_TUNING")) tune_load_file(path);
 }
 
@@ -709,6 +722,7 @@ int arena_init() { return ensure_device(); }
 
 SegPlan seg_plan(int kind, uint64_t n, uint64_t nseg) {
     SegPlan p{};
+    p.shape = seg_shape_for(kind, n, nseg);
     switch (kind) {
         case ORIGAMI_U32:
             p.maxl = seg_levels_u32(n);
@@ -743,10 +757,10 @@ cudaError_t seg_launch(int kind, void* d, void* tmp, const uint64_t* off, uint64
                        void* scratch, const SegPlan& p, cudaStream_t st) {
     const uint64_t m = key_mask(kind);
     switch (kind) {
-        case ORIGAMI_U32: return seg_sort_u32(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
+        case ORIGAMI_U32: return seg_sort_u32(d, tmp, off, nseg, n, m, scratch, p.maxl, p.shape, st);
         case ORIGAMI_U64:
-        case ORIGAMI_I64: return seg_sort_u64(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
-        default: return seg_sort_kv(d, tmp, off, nseg, n, m, scratch, p.maxl, st);
+        case ORIGAMI_I64: return seg_sort_u64(d, tmp, off, nseg, n, m, scratch, p.maxl, p.shape, st);
+        default: return seg_sort_kv(d, tmp, off, nseg, n, m, scratch, p.maxl, p.shape, st);
     }
 }
 }  // namespace origami
@@ -1061,6 +1075,89 @@ int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap) {
     char line[128];
     std::snprintf(line, sizeof line, "chosen fan=%d variant=%d size_class=%d\n", shape_fan(best), shape_variant(best),
                   size_class(n));
+    rep += line;
+    if (report && cap) {
+        std::strncpy(report, rep.c_str(), cap - 1);
+        report[cap - 1] = 0;
+    }
+    return ORIGAMI_OK;
+}
+
+
+// ---------------------------------------------------- segmented tuning --
+int origami_seg_tuning_get(int kind, uint64_t n, uint64_t nseg, int* shape) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (!shape) return fail(ORIGAMI_ERR_INVALID, "shape is NULL");
+    *shape = seg_shape_for(kind, n, nseg);
+    return ORIGAMI_OK;
+}
+
+int origami_seg_tuning_set(int kind, uint64_t n, uint64_t nseg, int shape) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (shape != 0 && shape != 1) return fail(ORIGAMI_ERR_INVALID, "shape must be 0 or 1");
+    std::call_once(g_tune_once, tune_init);
+    g_seg_tune[kind][seg_class(n, nseg)].store(shape, std::memory_order_relaxed);
+    return ORIGAMI_OK;
+}
+
+// Times both merge shapes of the segmented sort on the caller's own segments
+// (device buffers; d is restored to its input after every run) and stores the
+// faster for their mean segment length. Best of three after a warm-up each.
+int origami_autotune_segmented(int kind, void* d, void* tmp, const uint64_t* offsets, uint64_t nseg, uint64_t n,
+                               char* report, uint64_t cap) {
+    if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
+    if (nseg == 0 || n == 0) return fail(ORIGAMI_ERR_INVALID, "autotune needs segments");
+    if (!d || !tmp || !offsets) return fail(ORIGAMI_ERR_INVALID, "d, tmp and offsets are required");
+    if ((((uintptr_t)d) | ((uintptr_t)tmp)) & 15)
+        return fail(ORIGAMI_ERR_ALIGN, "segmented sort needs 16-byte aligned device buffers");
+    int rc = ensure_device();
+    if (rc != ORIGAMI_OK) return rc;
+    std::call_once(g_tune_once, tune_init);
+    const uint64_t bytes = n * item_bytes(kind);
+    cudaStream_t st = worker_stream();
+    SegPlan plan = seg_plan(kind, n, nseg);
+    void *keep = nullptr, *scratch = nullptr;
+    CK(cudaMallocAsync(&keep, bytes, st), "autotune buffers");
+    cudaError_t e = cudaMallocAsync(&scratch, plan.scratch_bytes, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(keep, d, bytes, cudaMemcpyDeviceToDevice, st);
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    std::string rep;
+    int best = 0;
+    float best_ms = 1e30f;
+    for (int shape = 0; shape < 2 && e == cudaSuccess; ++shape) {
+        plan.shape = shape;
+        float ms_best = 1e30f;
+        for (int it = 0; it < 4 && e == cudaSuccess; ++it) {
+            e = cudaMemcpyAsync(d, keep, bytes, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaEventRecord(a, st);
+            if (e == cudaSuccess) e = seg_launch(kind, d, tmp, offsets, nseg, n, scratch, plan, st);
+            if (e == cudaSuccess) e = cudaEventRecord(b, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0;
+            if (e == cudaSuccess && it > 0 && cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
+                ms_best = std::min(ms_best, ms);
+        }
+        char line[128];
+        std::snprintf(line, sizeof line, "shape=%d ms=%.4f\n", shape, ms_best);
+        rep += line;
+        if (ms_best < best_ms) {
+            best_ms = ms_best;
+            best = shape;
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, keep, bytes, cudaMemcpyDeviceToDevice, st);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (scratch) cudaFreeAsync(scratch, st);
+    cudaFreeAsync(keep, st);
+    const cudaError_t es = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "segmented autotune");
+    if (es != cudaSuccess) return cuda_fail(es, "segmented autotune");
+    g_seg_tune[kind][seg_class(n, nseg)].store(best, std::memory_order_relaxed);
+    char line[128];
+    std::snprintf(line, sizeof line, "chosen shape=%d mean_len_class=%d\n", best, seg_class(n, nseg));
     rep += line;
     if (report && cap) {
         std::strncpy(report, rep.c_str(), cap - 1);

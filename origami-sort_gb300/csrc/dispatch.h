@@ -35,7 +35,7 @@ ORIGAMI_DECLARE_SORT(kv)
     int seg_levels_##name(uint64_t n);                                                           \
     uint64_t seg_scratch_bytes_##name(uint64_t n, uint64_t nseg, int maxl);                      \
     cudaError_t seg_sort_##name(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n, \
-                                uint64_t key_mask, void* scratch, int maxl, cudaStream_t st);     \
+                                uint64_t key_mask, void* scratch, int maxl, int shape, cudaStream_t st); \
     int seg_err_offset_##name(uint64_t n, uint64_t nseg, int maxl);                               \
     int seg_prepare_##name(); /* one-time kernel attributes; call outside stream capture */
 ORIGAMI_DECLARE_SEG(u32)
@@ -52,6 +52,7 @@ struct SegPlan {
     int maxl;
     uint64_t scratch_bytes;
     int err_offset;
+    int shape;  // merge shape of the level merges (0 or 1), from the segmented tuning table
 };
 SegPlan seg_plan(int kind, uint64_t n, uint64_t nseg);
 void seg_prepare(int kind);

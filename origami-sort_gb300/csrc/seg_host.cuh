@@ -10,7 +10,7 @@ namespace origami {
 // Grids of the strided kernels: every SM full (resident CTAs per SM x SMs).
 template <class T>
 struct SegGrids {
-    int tile = 0, merge = 0, part = 0;
+    int tile = 0, merge[2] = {0, 0}, part = 0;  // merge: per merge shape
 };
 
 template <class T>
@@ -21,13 +21,18 @@ const SegGrids<T>& seg_grids() {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(seg_tile_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SegShape<T>::SMEM);
-        cudaFuncSetAttribute(seg_merge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)SegMergeShape<T>::SMEM);
+        cudaFuncSetAttribute(seg_merge_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)SegMergeShape<T, 0>::SMEM);
+        cudaFuncSetAttribute(seg_merge_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)SegMergeShape<T, 1>::SMEM);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_tile_kernel<T>, SegShape<T>::NTM, SegShape<T>::SMEM);
         const int tile = sms * (per > 0 ? per : 1);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T>, Config<T>::P_NT,
-                                                      SegMergeShape<T>::SMEM);
-        g.merge = sms * (per > 0 ? per : 1);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T, 0>, SegMergeCfg<T, 0>::NT,
+                                                      SegMergeShape<T, 0>::SMEM);
+        g.merge[0] = sms * (per > 0 ? per : 1);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_merge_kernel<T, 1>, SegMergeCfg<T, 1>::NT,
+                                                      SegMergeShape<T, 1>::SMEM);
+        g.merge[1] = sms * (per > 0 ? per : 1);
         g.part = sms * 8;
         g.tile = tile;
         return g;
@@ -41,13 +46,15 @@ int seg_grid() {
 }
 
 // Sorts every segment of d in place (result in d; tmp is the ping-pong
-// buffer). off: device array of nseg+1 offsets, off[nseg] == n.
+// buffer). off: device array of nseg+1 offsets, off[nseg] == n. shape: the
+// level merges' merge shape (SegMergeCfg).
 template <class T>
 cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t n, uint64_t xmask,
-                     void* scratch, int maxl, cudaStream_t st) {
+                     void* scratch, int maxl, int shape, cudaStream_t st) {
     if (nseg == 0) return cudaSuccess;
     SegState s = seg_state<T>(scratch, off, n, nseg, maxl);
     s.spin = wait_limit();
+    s.mtile = shape ? Config<T>::P2_TILE : Config<T>::P_TILE;
     const SegGrids<T>& g = seg_grids<T>();
     cudaMemsetAsync(s.err, 0, sizeof(int), st);
     const unsigned b = (unsigned)((nseg + 255) / 256);
@@ -66,7 +73,12 @@ cudaError_t seg_sort(T* d, T* tmp, const uint64_t* off, uint64_t nseg, uint64_t 
     for (int l = 0; l < maxl; ++l) {
         launch(n_part.c_str(), st, [&] { seg_part_kernel<T><<<g.part, 256, 0, st>>>(s, l, d, tmp); });
         launch(n_merge.c_str(), st, [&] {
-            seg_merge_kernel<T><<<g.merge, Config<T>::P_NT, SegMergeShape<T>::SMEM, st>>>(s, l, d, tmp, xmask);
+            if (shape)
+                seg_merge_kernel<T, 1><<<g.merge[1], SegMergeCfg<T, 1>::NT, SegMergeShape<T, 1>::SMEM, st>>>(
+                    s, l, d, tmp, xmask);
+            else
+                seg_merge_kernel<T, 0><<<g.merge[0], SegMergeCfg<T, 0>::NT, SegMergeShape<T, 0>::SMEM, st>>>(
+                    s, l, d, tmp, xmask);
         });
     }
     return cudaGetLastError();

@@ -83,6 +83,7 @@ struct SegState {
     uint32_t* tileseg;    // segment of each tile job
     int* err;             // 1 / 3 = a bulk-copy wait expired (bulk.cuh), 2 = bad offsets
     uint32_t spin;        // polls before a bulk-copy wait gives up
+    uint32_t mtile;       // merge tile of the level merges (the merge shape's, SegMergeCfg)
 };
 
 template <class T>
@@ -91,12 +92,14 @@ struct SegGeom {
     uint32_t tiles, levels, mtiles;
     // An invalid segment (decreasing offsets or past the buffer) is treated as
     // empty; the plan kernel reports it.
-    __device__ __forceinline__ SegGeom(const uint64_t* off, uint32_t s, uint64_t n) {
+    // mt: merge tile of the level merges (only mtiles depends on it)
+    __device__ __forceinline__ SegGeom(const uint64_t* off, uint32_t s, uint64_t n,
+                                       uint64_t mt = Config<T>::P_TILE) {
         const uint64_t a = off[s], b = off[s + 1];
         len = (a <= b && b <= n) ? b - a : 0;
         tiles = (uint32_t)((len + SegCfg<T>::TILE - 1) / SegCfg<T>::TILE);
         levels = (uint32_t)seg_levels_for<T>(len);
-        mtiles = (uint32_t)((len + Config<T>::P_TILE - 1) / Config<T>::P_TILE);
+        mtiles = (uint32_t)((len + mt - 1) / mt);
     }
 };
 
@@ -126,7 +129,7 @@ __global__ void seg_plan_kernel(SegState st) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= st.nseg) return;
     if (st.off[s + 1] < st.off[s] || st.off[s + 1] > st.n) atomicExch(st.err, 2);
-    const SegGeom<T> g(st.off, s, st.n);
+    const SegGeom<T> g(st.off, s, st.n, st.mtile);
     const uint32_t n = st.nseg;
     st.cnt[s] = g.tiles;
     for (int l = 0; l < st.maxl; ++l) st.cnt[(1 + l) * (size_t)n + s] = ((uint32_t)l < g.levels) ? g.mtiles : 0u;
@@ -376,7 +379,7 @@ __global__ void seg_part_kernel(SegState st, int l, const T* d, const T* tmp) {
          j += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t s = seg_of_job(pref, st.nseg, (uint32_t)j);
         const SegGeom<T> g(st.off, s, st.n);
-        const SegPair p(g.len, run, j - pref[s], Config<T>::P_TILE);
+        const SegPair p(g.len, run, j - pref[s], st.mtile);
         const uint64_t base = st.off[s] + p.pb;
         const T* A = seg_buf<const T>(g.levels, l, d, tmp) + base;
         st.splits[j] = global_merge_path_interp(A, (int64_t)p.la, A + p.la, (int64_t)p.lb, (int64_t)p.d0,
@@ -436,16 +439,33 @@ __device__ __forceinline__ SegBulkGeom seg_bulk_issue(T* stage, const T* d, cons
     return q;
 }
 
-template <class T>
-using SegMergeShape = PairBulkShape<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::STABLE, Config<T>::P_TILE>;
-
-template <class T>
-__global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_kernel(SegState st, int l, T* d,
-                                                                                       T* tmp, uint64_t xmask) {
+// Merge shapes of the level merges: 0 = the binary pass's first tile shape
+// (P_*), 1 = its second (P2_*, twice the tile). Chosen per plan by the
+// segmented tuning table (capi.cu), keyed by kind and mean segment length.
+template <class T, int SH>
+struct SegMergeCfg {
     using C = Config<T>;
-    using Sh = SegMergeShape<T>;
+    static constexpr int NT = SH ? C::P2_NT : C::P_NT;
+    static constexpr int VT = SH ? C::P2_VT : C::P_VT;
+    static constexpr int TILE = SH ? C::P2_TILE : C::P_TILE;
+    static constexpr int MINB = SH ? C::P2_MINB : C::P_MINB;
+    static constexpr bool STABLE = C::STABLE;
+};
+static_assert(2 * SegCfg<uint32_t>::TILE % Config<uint32_t>::P2_TILE == 0 &&
+                  2 * SegCfg<uint64_t>::TILE % Config<uint64_t>::P2_TILE == 0 &&
+                  2 * SegCfg<KV64>::TILE % Config<KV64>::P2_TILE == 0,
+              "a merge tile never straddles two run pairs");
+template <class T, int SH = 0>
+using SegMergeShape = PairBulkShape<T, SegMergeCfg<T, SH>::NT, SegMergeCfg<T, SH>::VT, Config<T>::STABLE,
+                                    SegMergeCfg<T, SH>::TILE>;
+
+template <class T, int SH>
+__global__ void __launch_bounds__(SegMergeCfg<T, SH>::NT, SegMergeCfg<T, SH>::MINB)
+    seg_merge_kernel(SegState st, int l, T* d, T* tmp, uint64_t xmask) {
+    using C = SegMergeCfg<T, SH>;
+    using Sh = SegMergeShape<T, SH>;
     constexpr int V = Vec<T>::N;
-    constexpr int VO = Block<T, C::P_VT, C::STABLE>::VO;
+    constexpr int VO = Block<T, C::VT, C::STABLE>::VO;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int split[Sh::In::SPLITS];
     __shared__ SegBulkGeom geom[2];
@@ -512,13 +532,13 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
         const int nblk = (tot + VO - 1) / VO;
         if (tid < nblk) split[tid] = merge_path_ix<T, LinIdx>(buf, q.as, q.na, q.bs, q.nb, tid * VO);
         __syncthreads();
-        T r[C::P_VT];
+        T r[C::VT];
         const int diag = tid * VO;
         const int cnt = tid < nblk ? min(VO, tot - diag) : 0;
         if (tid < nblk) {
             const int sa = split[tid];
             const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, C::P_VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r,
+            merge_block_regs<T, C::VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r,
                                                     q.as + q.na, q.bs + q.nb);
         }
         __syncthreads();
@@ -551,7 +571,7 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
             if (tid < head) op[q.sh + tid] = buf[q.sh + tid];
             else if (tid < head + tail) op[x1 + tid - head] = buf[x1 + tid - head];
         } else {
-            for (int i = tid; i < tot; i += C::P_NT) op[q.sh + i] = buf[q.sh + i];
+            for (int i = tid; i < tot; i += C::NT) op[q.sh + i] = buf[q.sh + i];
         }
     }
     if (tid == 0) bulk_wait_read<0>();
@@ -560,7 +580,7 @@ __global__ void __launch_bounds__(Config<T>::P_NT, Config<T>::P_MINB) seg_merge_
 // ------------------------------------------------------------ scratch ----
 template <class T>
 inline uint64_t seg_tile_slots(uint64_t n, uint64_t nseg) {
-    return n / Config<T>::P_TILE + nseg + 2;  // merge tiles of one level, upper bound
+    return n / Config<T>::P_TILE + nseg + 2;  // merge tiles of one level, upper bound (smaller shape)
 }
 
 // Tile jobs: every segment's tiles, upper bound.
@@ -604,6 +624,7 @@ inline SegState seg_state(void* scratch, const uint64_t* off, uint64_t n, uint64
     s.tileseg = reinterpret_cast<uint32_t*>(take(seg_tile_jobs<T>(n, nseg) * 4));
     s.claim = reinterpret_cast<unsigned*>(take(q * 4));
     s.spin = BULK_SPIN_LIMIT;
+    s.mtile = Config<T>::P_TILE;
     return s;
 }
 

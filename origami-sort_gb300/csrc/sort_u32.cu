@@ -43,9 +43,9 @@ uint64_t seg_scratch_bytes_u32(uint64_t n, uint64_t nseg, int maxl) {
 }
 
 cudaError_t seg_sort_u32(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
-                          uint64_t key_mask, void* scratch, int maxl, cudaStream_t st) {
+                          uint64_t key_mask, void* scratch, int maxl, int shape, cudaStream_t st) {
     return seg_sort<uint32_t>(static_cast<uint32_t*>(d), static_cast<uint32_t*>(tmp), off, nseg, n, key_mask, scratch,
-                          maxl, st);
+                          maxl, shape, st);
 }
 
 int seg_prepare_u32() { return seg_grid<uint32_t>(); }

@@ -43,9 +43,9 @@ uint64_t seg_scratch_bytes_u64(uint64_t n, uint64_t nseg, int maxl) {
 }
 
 cudaError_t seg_sort_u64(void* d, void* tmp, const uint64_t* off, uint64_t nseg, uint64_t n,
-                          uint64_t key_mask, void* scratch, int maxl, cudaStream_t st) {
+                          uint64_t key_mask, void* scratch, int maxl, int shape, cudaStream_t st) {
     return seg_sort<uint64_t>(static_cast<uint64_t*>(d), static_cast<uint64_t*>(tmp), off, nseg, n, key_mask, scratch,
-                          maxl, st);
+                          maxl, shape, st);
 }
 
 int seg_prepare_u64() { return seg_grid<uint64_t>(); }

@@ -113,6 +113,12 @@ def lib():
         L.origami_serve_destroy.argtypes = [vp]
         L.origami_autotune.restype = i
         L.origami_autotune.argtypes = [i, u64, ctypes.c_char_p, u64]
+        L.origami_autotune_segmented.restype = i
+        L.origami_autotune_segmented.argtypes = [i, vp, vp, vp, u64, u64, ctypes.c_char_p, u64]
+        L.origami_seg_tuning_get.restype = i
+        L.origami_seg_tuning_get.argtypes = [i, u64, u64, ctypes.POINTER(i)]
+        L.origami_seg_tuning_set.restype = i
+        L.origami_seg_tuning_set.argtypes = [i, u64, u64, i]
         L.origami_tuning_get.restype = i
         L.origami_tuning_get.argtypes = [i, u64, ctypes.POINTER(i), ctypes.POINTER(i)]
         L.origami_tuning_set.restype = i
@@ -347,6 +353,32 @@ def autotune(kind, n):
     check(lib().origami_autotune(k, n, buf, len(buf)))
     fan, var = tuning_get(k, n)
     return {"fan": fan, "variant": var, "report": buf.value.decode()}
+
+
+def autotune_segmented(d, tmp, offsets, kind):
+    """Time both merge shapes of the segmented sort on these device segments
+    (d is left holding its input); the faster becomes the default for their
+    mean segment length. Returns {"shape", "report"}."""
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    p, n = _ptr_len(d, k)
+    nseg = offsets.numel() - 1
+    buf = ctypes.create_string_buffer(1024)
+    check(lib().origami_autotune_segmented(k, p, tmp.data_ptr(), offsets.data_ptr(), nseg, n, buf, len(buf)))
+    return {"shape": seg_tuning_get(k, n, nseg), "report": buf.value.decode()}
+
+
+def seg_tuning_get(kind, n, nseg):
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    v = ctypes.c_int()
+    check(lib().origami_seg_tuning_get(k, n, nseg, ctypes.byref(v)))
+    return v.value
+
+
+def seg_tuning_set(kind, n, nseg, shape):
+    """Merge shape (0 or 1) of segmented sorts whose mean segment length falls
+    in the size class of n / nseg."""
+    k = KIND_NAMES[kind] if isinstance(kind, str) else int(kind)
+    check(lib().origami_seg_tuning_set(k, n, nseg, shape))
 
 
 def tuning_get(kind, n):

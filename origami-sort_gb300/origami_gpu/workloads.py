@@ -84,6 +84,11 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
     tmp = torch.empty_like(pristine)
     offs = torch.from_numpy(off).to(dev)
     stream = torch.cuda.current_stream(dev)
+    # the segmented tuning table's merge shape for these segments, timed on them
+    # (outside the measurement); the plan takes its shape from the table
+    from . import autotune_segmented
+    d.copy_(pristine)
+    tuning = autotune_segmented(d, tmp, offs, U32)
     plan = SegmentedPlan(d, offs, tmp, kind=U32)
     for _ in range(warmup):
         d.copy_(pristine)
@@ -150,7 +155,7 @@ def batched(torch, steps=5, warmup=3, nseg=65536, lo=32, hi=1 << 20, seed=4, loo
                     f"keys uniform (torch seed {seed}); {n} keys in total",
         "keys": n, "segments": nseg, "correct": ok,
         "segmented_graph_ms": seg_ms, "segmented_gkeys_s": n / seg_ms / 1e6,
-        "kernels_per_replay": seg_launches, "kernels": kernels,
+        "kernels_per_replay": seg_launches, "kernels": kernels, "tuning": tuning,
         "loop_plain_ms": loop_ms, "loop_plain_gkeys_s": n / loop_ms / 1e6,
         "speedup_vs_loop": loop_ms / seg_ms,
         "cpu_segments": cpu,

@@ -153,3 +153,15 @@ def test_wait_limit_is_host_state(lib):
     assert lib.origami_set_wait_limit(77) == og.OK
     assert lib.origami_get_wait_limit() == 77
     assert lib.origami_set_wait_limit(default) == og.OK
+
+
+def test_segmented_tuning_table(lib):
+    assert og.seg_tuning_get(og.U32, 1 << 24, 1 << 10) == 0  # default: the first merge shape
+    og.seg_tuning_set(og.U32, 1 << 24, 1 << 10, 1)
+    assert og.seg_tuning_get(og.U32, (1 << 24) + 5, 1 << 10) == 1  # same mean-length class
+    assert og.seg_tuning_get(og.U32, 1 << 20, 1 << 10) == 0
+    og.seg_tuning_set(og.U32, 1 << 24, 1 << 10, 0)
+    with pytest.raises(og.OrigamiError):
+        og.seg_tuning_set(og.U32, 100, 1, 2)
+    with pytest.raises(og.OrigamiError):
+        og.seg_tuning_set(9, 100, 1, 0)

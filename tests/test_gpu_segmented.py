@@ -145,3 +145,42 @@ def test_segmented_graph_plan(kind):
         plan.status(s)
         assert np.array_equal(d.cpu().numpy().view(a.dtype), want)
     plan.close()
+
+
+@pytest.mark.parametrize("kind", [og.U32, og.U64, og.I64, og.KV64, og.KVU64])
+@pytest.mark.parametrize("shape", [0, 1])
+def test_segmented_merge_shapes(kind, shape):
+    # both merge shapes of the level merges give the exact per-segment sort
+    rng = np.random.default_rng(300 + kind)
+    lens = lengths(kind, rng, 120)
+    rng.shuffle(lens)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    n, nseg = int(off[-1]), len(lens)
+    a = make_items(kind, n, seed=kind + 90, dist="few" if shape else "uniform")
+    before = og.seg_tuning_get(kind, n, nseg)
+    og.seg_tuning_set(kind, n, nseg, shape)
+    try:
+        assert og.seg_tuning_get(kind, n, nseg) == shape
+        got = run_device(a, off, kind)
+    finally:
+        og.seg_tuning_set(kind, n, nseg, before)
+    assert np.array_equal(got, expected(a, off))
+
+
+@pytest.mark.parametrize("kind", [og.U32, og.KV64])
+def test_segmented_autotune(kind):
+    rng = np.random.default_rng(17)
+    lens = rng.integers(1 << 12, 1 << 16, 64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    a = make_items(kind, int(off[-1]), seed=18)
+    d = torch.from_numpy(a.view(np.uint8).copy()).cuda()
+    tmp = torch.empty_like(d)
+    o = torch.from_numpy(off.astype(np.int64)).cuda()
+    r = og.autotune_segmented(d, tmp, o, kind)
+    assert r["shape"] in (0, 1)
+    assert r["report"].count("shape=") == 3  # two timings and the choice
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy().view(a.dtype), a)  # the input is left in d
+    og.sort_segmented(d, o, kind=kind)
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy().view(a.dtype), expected(a, off))
