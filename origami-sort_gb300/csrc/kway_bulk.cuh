@@ -418,7 +418,7 @@ __device__ __forceinline__ void kb_merge_tile(T* buf, int (*geo)[2][KWAY_MAX], i
         if (p >= 0) {
             const int sa = split[tid];
             const int ea = (tid - first + 1 < nbp) ? split[tid + 1] : la;
-            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r, a0 + la, b0 + lb);
+            merge_block_regs<T, VT, STABLE>(buf, a0 + sa, b0 + (diag - sa), ea - sa, cnt, r);
         }
         // next round's geometry (the other buffer; nothing reads it this round)
         if (tid < npairs) {

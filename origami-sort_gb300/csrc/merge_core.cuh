@@ -8,14 +8,11 @@
 // ends from the next block's search, so its outputs are exactly the merge of
 // A[a0, a1) and B[b0, b1).
 //
-//  keys only  - VO = VT - 1. The thread loads A[a0, a1) ascending, then one
-//               more item, then B[b0, b1) descending into VT registers (a
+//  keys only  - VO = VT - 1. The thread loads A[a0, a1) ascending, then the
+//               largest key, then B[b0, b1) descending into VT registers (a
 //               bitonic sequence) and sorts it with a bitonic half-cleaner
 //               network (VT/2*log2(VT) compare-exchanges); the loads are
-//               independent of each other. The extra item is A[a1] or B[b1],
-//               whichever exists (either is >= every output of the block), so
-//               each slot loads from a computed address with no mask; only a
-//               block at the end of both lists fills it with the largest key.
+//               independent of each other.
 //  stable     - (key-value items) VO = VT. The thread merges serially, A first
 //               on equal keys, so equal keys keep their input order.
 //
@@ -70,37 +67,11 @@ __device__ __forceinline__ int merge_path_ix(const T* s, int a0, int na, int b0,
     return lo;
 }
 
-// Keys: the block's bitonic register sequence. Slots [0, lim) hold A[ia0 ..]
-// ascending, the others B[.. ib0] descending (slot i holds B[ib0 + VT-1 - i]),
-// lim = na + 1 when A has an item after the block's part, else na (slot na
-// then holds B's next item). A block with neither (the end of both lists, or a
-// short block) masks: slots between the parts hold the largest key.
-template <class T, int VT, class IX>
-__device__ __forceinline__ void load_bitonic(const T* src, int ia0, int ib0, int na, int cnt, int a_end, int b_end,
-                                             T (&v)[VT]) {
-    const int nb = cnt - na;
-    const int pb = ib0 + VT - 1;
-    const bool a_more = ia0 + na < a_end, b_more = ib0 + nb < b_end;
-    if (cnt == VT - 1 && (a_more || b_more)) {
-        const int lim = a_more ? na + 1 : na;
-#pragma unroll
-        for (int i = 0; i < VT; ++i) v[i] = src[IX::at(i < lim ? ia0 + i : pb - i)];
-    } else {
-#pragma unroll
-        for (int i = 0; i < VT; ++i) {
-            const bool fromA = i < na;
-            const T t = src[IX::at(fromA ? ia0 + i : pb - i)];
-            v[i] = (fromA || i >= VT - nb) ? t : Traits<T>::max_item();
-        }
-    }
-}
-
 // Merges one block: cnt outputs at dst[o..], na of them from A starting at
-// src index ia0, the rest from B starting at ib0; A ends at src index a_end and
-// B at b_end.
+// src index ia0, the rest from B starting at ib0.
 template <class T, int VT, bool STABLE, class IX>
-__device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int ib0, int na, int cnt, int o,
-                                            int a_end, int b_end) {
+__device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int ib0, int na, int cnt,
+                                            int o) {
     const int nb = cnt - na;
     if constexpr (STABLE) {
         int ia = ia0, ib = ib0;
@@ -120,7 +91,14 @@ __device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int i
         }
     } else {
         T v[VT];
-        load_bitonic<T, VT, IX>(src, ia0, ib0, na, cnt, a_end, b_end, v);
+        const int pb = ib0 + VT - 1;  // B is read backwards: slot i holds B[pb - i]
+#pragma unroll
+        for (int i = 0; i < VT; ++i) {
+            const bool fromA = i < na;
+            const T t = src[IX::at(fromA ? ia0 + i : pb - i)];
+            // slots between the A part and the B part hold the largest key
+            v[i] = (fromA || i >= VT - nb) ? t : Traits<T>::max_item();
+        }
         bitonic_clean<T, VT>(v);
         if (cnt == VT - 1) {
 #pragma unroll
@@ -137,8 +115,7 @@ __device__ __forceinline__ void merge_block(const T* src, T* dst, int ia0, int i
 // that the caller can overwrite the source buffer once every thread is done
 // reading it.
 template <class T, int VT, bool STABLE>
-__device__ __forceinline__ void merge_block_regs(const T* src, int ia0, int ib0, int na, int cnt, T (&out)[VT],
-                                                 int a_end, int b_end) {
+__device__ __forceinline__ void merge_block_regs(const T* src, int ia0, int ib0, int na, int cnt, T (&out)[VT]) {
     const int nb = cnt - na;
     if constexpr (STABLE) {
         int ia = ia0, ib = ib0;
@@ -157,7 +134,13 @@ __device__ __forceinline__ void merge_block_regs(const T* src, int ia0, int ib0,
             }
         }
     } else {
-        load_bitonic<T, VT, LinIdx>(src, ia0, ib0, na, cnt, a_end, b_end, out);
+        const int pb = ib0 + VT - 1;  // B is read backwards: slot i holds B[pb - i]
+#pragma unroll
+        for (int i = 0; i < VT; ++i) {
+            const bool fromA = i < na;
+            const T t = src[fromA ? ia0 + i : pb - i];
+            out[i] = (fromA || i >= VT - nb) ? t : Traits<T>::max_item();
+        }
         bitonic_clean<T, VT>(out);
     }
 }
@@ -189,7 +172,7 @@ __device__ __forceinline__ void merge_round_uniform(const T* src, T* dst, int w,
         if (cnt <= 0) continue;
         const int sa = split[blk];
         const int ea = (blk + 1 < (p + 1) * bpp) ? split[blk + 1] : (b0 - a0);
-        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag, b0, e0);
+        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag);
     }
     __syncthreads();
 }
@@ -243,7 +226,7 @@ __device__ __forceinline__ void merge_round_lists(const T* src, T* dst, const in
         const int cnt = min(VO, e0 - a0 - diag);
         const int sa = split[blk];
         const int ea = (blk + 1 < next) ? split[blk + 1] : (b0 - a0);
-        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag, b0, e0);
+        merge_block<T, VT, STABLE, IX>(src, dst, a0 + sa, b0 + (diag - sa), ea - sa, cnt, a0 + diag);
     }
     __syncthreads();
 }
@@ -266,7 +249,7 @@ __device__ __forceinline__ void merge_pair_round(const T* src, int as, int na, i
         const int cnt = min(VO, total - diag);
         const int sa = split[blk];
         const int ea = (blk + 1 < nblk) ? split[blk + 1] : na;
-        merge_block<T, VT, STABLE, LinIdx>(src, dst, as + sa, bs + (diag - sa), ea - sa, cnt, diag, as + na, bs + nb);
+        merge_block<T, VT, STABLE, LinIdx>(src, dst, as + sa, bs + (diag - sa), ea - sa, cnt, diag);
     }
     __syncthreads();
 }
@@ -290,7 +273,7 @@ __device__ __forceinline__ void merge_pair_round_inplace(T* buf, int as, int na,
     if (tid < nblk) {
         const int sa = split[tid];
         const int ea = (tid + 1 < nblk) ? split[tid + 1] : na;
-        merge_block_regs<T, VT, STABLE>(buf, as + sa, bs + (diag - sa), ea - sa, cnt, r, as + na, bs + nb);
+        merge_block_regs<T, VT, STABLE>(buf, as + sa, bs + (diag - sa), ea - sa, cnt, r);
     }
     __syncthreads();
     if (cnt == VO) {

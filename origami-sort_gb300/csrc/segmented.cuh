@@ -538,8 +538,7 @@ __global__ void __launch_bounds__(SegMergeCfg<T, SH>::NT, SegMergeCfg<T, SH>::MI
         if (tid < nblk) {
             const int sa = split[tid];
             const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, C::VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r,
-                                                    q.as + q.na, q.bs + q.nb);
+            merge_block_regs<T, C::VT, C::STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
         }
         __syncthreads();
         // stage index x holds output item x - sh, so x = 0 lies on a 16-byte

@@ -473,8 +473,7 @@ __global__ void __launch_bounds__(NT, MINB)
         if (tid < nblk) {
             const int sa = split[tid];
             const int ea = (tid + 1 < nblk) ? split[tid + 1] : q.na;
-            merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r, q.as + q.na,
-                                            q.bs + q.nb);
+            merge_block_regs<T, VT, STABLE>(buf, q.as + sa, q.bs + (diag - sa), ea - sa, cnt, r);
         }
         __syncthreads();
         if (cnt == VO) {
