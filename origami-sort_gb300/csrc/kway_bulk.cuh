@@ -59,7 +59,7 @@ template <class T>
 struct KbCfg;
 template <>
 struct KbCfg<uint32_t> {
-    static constexpr int S = 64, M = 64, NT = 192, VT = 32, MINB = 4;
+    static constexpr int S = 64, M = 48, NT = 160, VT = 32, MINB = 6;
 };
 template <>
 struct KbCfg<uint64_t> {
