@@ -63,7 +63,7 @@ struct KbCfg<uint32_t> {
 };
 template <>
 struct KbCfg<uint64_t> {
-    static constexpr int S = 32, M = 64, NT = 192, VT = 16, MINB = 4;
+    static constexpr int S = 32, M = 48, NT = 160, VT = 16, MINB = 5;
 };
 template <>
 struct KbCfg<KV64> {
