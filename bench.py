@@ -216,20 +216,35 @@ def job_gkeys_per_s(n, steps, world, total_ms):
 def short_workloads(torch):
     """Batched and serving measurements carried on the headline line (shorter
     runs than `--workload batched|serving`). Failures are reported, not raised."""
+    import origami_gpu as og
     from origami_gpu import workloads as wl
     out = {}
+
+    def fresh():
+        # each workload starts with the device memory the previous ones cached
+        # (torch's allocator, the library's pool) handed back: serving latency
+        # measured right after gigabytes of cached blocks on the default stream
+        # was 2-6x worse at p99 than in a fresh process
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        og.lib().origami_arena_trim()
+
+    fresh()
     try:
         out["batched"] = wl.batched(torch, steps=3, warmup=3)
     except Exception as e:  # reported in the line
         out["batched"] = {"error": repr(e)}
+    fresh()
     try:
         out["plain_configs"] = wl.plain_configs(torch)
     except Exception as e:
         out["plain_configs"] = {"error": repr(e)}
+    fresh()
     try:
         out["kv_distributions"] = wl.kv_distributions(torch, steps=2, warmup=1)
     except Exception as e:
         out["kv_distributions"] = {"error": repr(e)}
+    fresh()
     try:
         # one rate, long enough for a steady p99 (the rate sweep is --workload serving)
         sv = wl.serving(torch, rates=(400,), duration_s=5.0, pool_size=64)
@@ -296,7 +311,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="origami", choices=["origami", "reference"])
     ap.add_argument("--n", type=int, default=N_KEYS)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip timing the pass shapes before the measurement (the default shape is used)")

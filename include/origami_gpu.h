@@ -332,8 +332,9 @@ int origami_generate_device(int kind, void* d, uint64_t n, int dist, uint64_t se
  *                      receives one "fan= variant= ms=" line per shape.
  *   get / set          read or write one entry.
  *   save / load        the non-default entries as "kind class fan variant"
- *                      lines. The file named by ORIGAMI_TUNING, if set, is
- *                      loaded at first use.
+ *                      lines, and the segmented table's (below) as
+ *                      "seg kind class shape" lines. The file named by
+ *                      ORIGAMI_TUNING, if set, is loaded at first use.
  */
 int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap);
 int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant);

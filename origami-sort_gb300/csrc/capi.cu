@@ -628,12 +628,22 @@ int sort_host_direct(int kind, void* host_in, void* host_out, const void* vin, v
     return rc;
 }
 
-// Table entries of a tuning file: one "kind size_class fan variant" line each.
+// Tuning file: one entry per line. "kind class fan variant": the plain sort's
+// pass shape for a size class; "seg kind class shape": the segmented sort's
+// merge shape for a class of mean segment length. Other lines are skipped.
 int tune_load_file(const char* path) {
     FILE* f = std::fopen(path, "r");
     if (!f) return fail(ORIGAMI_ERR_INVALID, "cannot open tuning file %s", path);
+    char line[256];
     int kind, cls, fan, var, loaded = 0;
-    while (std::fscanf(f, "%d %d %d %d", &kind, &cls, &fan, &var) == 4) {
+    while (std::fgets(line, sizeof line, f)) {
+        if (std::sscanf(line, "seg %d %d %d", &kind, &cls, &var) == 3) {
+            if (kind < 0 || kind > 4 || cls < 0 || cls >= TUNE_CLASSES || (var != 0 && var != 1)) continue;
+            g_seg_tune[kind][cls].store(var, std::memory_order_relaxed);
+            ++loaded;
+            continue;
+        }
+        if (std::sscanf(line, "%d %d %d %d", &kind, &cls, &fan, &var) != 4) continue;
         if (kind < 0 || kind > 4 || cls < 0 || cls >= TUNE_CLASSES) continue;
         if (fan != 2 && fan != 4 && fan != 8 && fan != 16) continue;
         if (var < 0 || var > 2 || (fan != 2 && var != 0)) continue;
@@ -1001,6 +1011,11 @@ int origami_tuning_save(const char* path) {
         for (int c = 0; c < TUNE_CLASSES; ++c) {
             const int code = g_tune[k][c].load(std::memory_order_relaxed);
             if (code != shape_code(2, 0)) std::fprintf(f, "%d %d %d %d\n", k, c, shape_fan(code), shape_variant(code));
+        }
+    for (int k = 0; k < 5; ++k)
+        for (int c = 0; c < TUNE_CLASSES; ++c) {
+            const int shape = g_seg_tune[k][c].load(std::memory_order_relaxed);
+            if (shape != 0) std::fprintf(f, "seg %d %d %d\n", k, c, shape);
         }
     std::fclose(f);
     return ORIGAMI_OK;

@@ -165,3 +165,15 @@ def test_segmented_tuning_table(lib):
         og.seg_tuning_set(og.U32, 100, 1, 2)
     with pytest.raises(og.OrigamiError):
         og.seg_tuning_set(9, 100, 1, 0)
+
+
+def test_segmented_tuning_in_the_tuning_file(lib, tmp_path):
+    # the segmented table travels in the same file as the plain sort's
+    og.seg_tuning_set(og.KV64, 1 << 22, 1 << 6, 1)  # mean length 2^16
+    path = tmp_path / "tune.txt"
+    og.tuning_save(path)
+    assert "seg 3 16 1" in path.read_text().split("\n")
+    og.seg_tuning_set(og.KV64, 1 << 22, 1 << 6, 0)
+    og.tuning_load(path)
+    assert og.seg_tuning_get(og.KV64, 1 << 16, 1) == 1
+    og.seg_tuning_set(og.KV64, 1 << 22, 1 << 6, 0)
