@@ -237,13 +237,14 @@ def test_merge_series(kind, merge_start, sort_n):
 
 @pytest.mark.parametrize("kind,n", [(og.U32, 1 << 26), (og.U64, 1 << 25), (og.KV64, 1 << 24),
                                     (og.U32, (1 << 28) + 12345)])
-def test_large_against_torch_sort(kind, n):
+@pytest.mark.parametrize("min_k", [0, 16])  # the tuned (binary) passes, and 16-way passes
+def test_large_against_torch_sort(kind, n, min_k):
     g = torch.Generator(device="cuda").manual_seed(11)
     words = 4 if kind == og.U32 else (8 if kind == og.U64 else 16)
     raw = torch.randint(0, 256, (n * words,), dtype=torch.uint8, device="cuda", generator=g)
     keep = raw.clone()
     tmp = torch.empty_like(raw)
-    out = og.sort(raw, tmp, kind=kind)
+    out = og.sort(raw, tmp, kind=kind, min_k=min_k)
     torch.cuda.synchronize()
     if kind == og.U32:
         k_in = keep.view(torch.int32).to(torch.int64) & 0xFFFFFFFF
