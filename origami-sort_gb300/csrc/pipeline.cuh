@@ -28,6 +28,7 @@ struct Config<uint32_t> {
     static constexpr bool WARP_K1 = true;
     // 8 warps sort 1024 keys each; 9 warps share the merge rounds (265 blocks)
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 32, K1_MINB = 3;
+    static constexpr int K1_RUN0 = 1024;  // register merges up to the whole warp's 1024 keys
     static constexpr int K1_NT = 256, K1_VTS = 32, K1_VTM = 32;  // (block K1, unused)
     // binary pass tiles (P_BULK: the persistent bulk-copy merge kernel)
     static constexpr int P_NT = 160, P_VT = 32, P_TILE = 4096, P_MINB = 6;
@@ -41,6 +42,7 @@ template <>
 struct Config<uint64_t> {
     static constexpr bool WARP_K1 = true;
     static constexpr int K1_NW = 8, K1_NWT = 9, K1_VT = 16, K1_MINB = 3;
+    static constexpr int K1_RUN0 = 128;  // register merges to runs of 128 keys, shared-memory rounds from there
     static constexpr int K1_NT = 512, K1_VTS = 8, K1_VTM = 16;
     static constexpr int P_NT = 160, P_VT = 16, P_TILE = 2048, P_MINB = 6;
     static constexpr bool P_BULK = true;
@@ -53,6 +55,7 @@ template <>
 struct Config<KV64> {
     static constexpr bool WARP_K1 = false;  // key-value items need stable merges
     static constexpr int K1_NW = 8, K1_NWT = 8, K1_VT = 8, K1_MINB = 1;
+    static constexpr int K1_RUN0 = 256;  // (the warp tile sort serves keys-only items)
     static constexpr int K1_NT = 256, K1_VTS = 8, K1_VTM = 11;  // 2048 items (32 KiB), serial blocks of 11
     static constexpr int P_NT = 96, P_VT = 11, P_TILE = 1024, P_MINB = 4;  // serial merge blocks of 11
     static constexpr bool P_BULK = true;
@@ -354,9 +357,9 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
     // kernel attributes, once per process (thread-safe static initialisation)
     static const bool configured = [] {
         if constexpr (C::WARP_K1) {
-            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>,
+            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, false, C::K1_RUN0>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
-            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true>,
+            cudaFuncSetAttribute(warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true, C::K1_RUN0>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k1_smem<T>());
         } else
             cudaFuncSetAttribute(block_sort_kernel<T, C::K1_NT, C::K1_VTS, C::K1_VTM, C::STABLE>,
@@ -390,7 +393,7 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per, warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>, C::K1_NWT * 32,
+                &per, warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, false, C::K1_RUN0>, C::K1_NWT * 32,
                 k1_smem<T>());
             return (uint32_t)(sms * (per > 0 ? per : 1));
         }();
@@ -409,11 +412,11 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         launch(n_k1.c_str(), st, [&] {
             if constexpr (C::WARP_K1) {
                 if (k1_samp)
-                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true>
+                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, true, C::K1_RUN0>
                         <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
                             in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err, k1_samp, k1_ssamp);
                 else
-                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB>
+                    warp_block_sort_kernel<T, C::K1_NW, C::K1_VT, C::K1_NWT, C::K1_MINB, false, C::K1_RUN0>
                         <<<(unsigned)tiles1, C::K1_NWT * 32, k1_smem<T>(), st>>>(
                             in, k1_out, n, k1_chunk, xin, passes == 0 ? xout : 0, ahead, err);
             } else

@@ -39,6 +39,7 @@ struct SegCfg<uint32_t> {
     static constexpr int VTM = VT;  // (stable rounds only)
     static constexpr int NWT = 9;  // warps in the shared-memory rounds (one merge block per thread)
     static constexpr int TILE_MINB = 3;  // CTAs per SM the register budget allows
+    static constexpr int RUN0 = 1024;    // register merges up to the warp's whole run
 };
 template <>
 struct SegCfg<uint64_t> {
@@ -48,6 +49,7 @@ struct SegCfg<uint64_t> {
     static constexpr int VTM = VT;
     static constexpr int NWT = 9;
     static constexpr int TILE_MINB = 2;
+    static constexpr int RUN0 = 128;  // register merges to runs of 128, shared-memory rounds from there
 };
 template <>
 struct SegCfg<KV64> {
@@ -57,6 +59,7 @@ struct SegCfg<KV64> {
     static constexpr int VTM = 11;  // serial merge blocks of the shared-memory rounds
     static constexpr int NWT = 8;
     static constexpr int TILE_MINB = 3;
+    static constexpr int RUN0 = 8;  // (stable tiles sort in registers, then merge rounds)
 };
 
 // Merge levels for a segment of len items (runs of TILE doubled until one).
@@ -204,6 +207,8 @@ __device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
     using C = SegCfg<T>;
     using Sh = SegShape<T>;
     constexpr int NT = Sh::NT, NTM = Sh::NTM, VT = C::VT, TILE = C::TILE, WT = 32 * VT;
+    constexpr int R0 = C::RUN0 < WT ? C::RUN0 : WT;  // runs the register merges stop at
+    static_assert((R0 & (R0 - 1)) == 0 && R0 >= VT, "runs of a power of two, at least one lane's");
     T* sa = reinterpret_cast<T*>(smem);
     T* sb = reinterpret_cast<T*>(smem + Sh::BUF_BYTES);
     const int tid = threadIdx.x;
@@ -269,17 +274,17 @@ __device__ bool seg_tile_sort(const T* src, T* dst, uint64_t p0, int cnt, uint64
                 const int i = w0 + k * 32 + lane;
                 v[k] = (i < cnt) ? Traits<T>::flip(sb[sh + i], xin) : Traits<T>::max_item();
             }
-            warp_sort<T, VT>(v, WT);
+            warp_sort<T, VT>(v, R0);
 #pragma unroll
             for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
         }
         __syncthreads();
-        if (span > WT) {
+        if (span > R0) {
             const T* s0 = sa;
             T* s1 = sb;
-            for (int w = WT; w < span; w <<= 1) {
+            for (int w = R0; w < span; w <<= 1) {
                 T* out = (2 * w >= span) ? s1 + sh : s1;  // the last round writes shifted
-                if (w == WT)
+                if (w == R0)
                     merge_round_uniform<T, NTM, VT, false, PadIdx<T>>(s0, out, w, span, split);
                 else
                     merge_round_uniform<T, NTM, VT, false, LinIdx>(s0, out, w, span, split);

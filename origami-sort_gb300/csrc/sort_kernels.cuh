@@ -110,7 +110,6 @@ struct WarpSortShape {
     static constexpr int WTILE = 32 * VT;
     static constexpr int BUF = padded_items<T>(TILE + VT + 1);
     static constexpr int VTM = VT;  // merge blocks of VT-1 outputs
-    static constexpr int SPLITS = TILE / (VTM - 1) + TILE / (2 * WTILE) + 4;
     static constexpr size_t SMEM = 2 * (((size_t)BUF * sizeof(T) + 15) & ~(size_t)15);
 };
 
@@ -120,7 +119,7 @@ struct WarpSortShape {
 // the first thread. SAMPLES: also writes the samples of the sorted tiles to
 // samp / ssamp for a k-way pass that follows (kway_bulk.cuh); a separate
 // instantiation, so that the plain tile sort keeps its registers.
-template <class T, int NW, int VT, int NWT = NW, int MINB = 1, bool SAMPLES = false>
+template <class T, int NW, int VT, int NWT = NW, int MINB = 1, bool SAMPLES = false, int RUN0 = 32 * VT>
 __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T* __restrict__ in,
                                                                         T* __restrict__ out, uint64_t n,
                                                                         int chunk, uint64_t xin,
@@ -131,10 +130,14 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
     using Sh = WarpSortShape<T, NW, VT, NWT>;
     static_assert(NWT >= NW, "the sorting warps take part in the merge rounds");
     constexpr int TILE = Sh::TILE, WT = Sh::WTILE;
+    // runs the warps' register merges stop at; shared-memory rounds take over
+    constexpr int R0 = RUN0 < WT ? RUN0 : WT;
+    static_assert((R0 & (R0 - 1)) == 0 && R0 >= VT, "runs of a power of two, at least one lane's");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sa = reinterpret_cast<T*>(smem_raw);
     T* sb = reinterpret_cast<T*>(smem_raw + Sh::SMEM / 2);
-    __shared__ int split[Sh::SPLITS];
+    // blocks of a round: at most TILE / (VT - 1) plus one partial block per pair
+    __shared__ int split[TILE / (VT - 1) + TILE / (2 * R0) + 4];
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const uint64_t base = (uint64_t)blockIdx.x * TILE;
@@ -172,18 +175,18 @@ __global__ void __launch_bounds__(NWT * 32, MINB) warp_block_sort_kernel(const T
                     v[j * V + k] = (i0 + k < valid) ? Traits<T>::flip(src[k], xin) : Traits<T>::max_item();
             }
         }
-        warp_sort<T, VT>(v, chunk);
+        warp_sort<T, VT>(v, chunk < R0 ? chunk : R0);
     }
-    if (WT < TILE && WT < chunk) {
+    if (R0 < TILE && R0 < chunk) {
         if (sorter) {
 #pragma unroll
             for (int k = 0; k < VT; ++k) sa[pad<T>(w0 + lane * VT + k)] = v[k];
         }
         __syncthreads();
-        merge_round_uniform<T, Sh::NTM, VT, false, PadIdx<T>>(sa, sb, WT, TILE, split);
+        merge_round_uniform<T, Sh::NTM, VT, false, PadIdx<T>>(sa, sb, R0, TILE, split);
         T* src = sb;
         T* dst = sa;
-        for (int w = 2 * WT; w < TILE && w < chunk; w <<= 1) {
+        for (int w = 2 * R0; w < TILE && w < chunk; w <<= 1) {
             merge_round_uniform<T, Sh::NTM, VT, false, LinIdx>(src, dst, w, TILE, split);
             T* t = src;
             src = dst;
