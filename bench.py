@@ -37,6 +37,7 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 N_KEYS = 1 << 28
 METRIC = "Gkeys/s sorting 1 GB uint32 on 1 GB300 (% HBM roofline); batched p50/p99 latency"
+PROFILE_EVERY = 7  # time every 7th launch of each kernel inside the timed steps
 WORKLOAD = "full sort of 268,435,456 uint32 keys (1 GiB), uniform over [0, 2^32)"
 
 
@@ -254,10 +255,18 @@ def short_workloads(torch):
         out["kv_distributions"] = wl.kv_distributions(torch, steps=2, warmup=1)
     except Exception as e:
         out["kv_distributions"] = {"error": repr(e)}
-    fresh()
     try:
-        # one rate, long enough for a steady p99 (the rate sweep is --workload serving)
-        sv = wl.serving(torch, rates=(400,), duration_s=5.0, pool_size=64)
+        # one rate, long enough for a steady p99 (the rate sweep is --workload
+        # serving), in a process of its own as a server would run: measured in
+        # this process after the other workloads, p99 and saturation varied
+        # 2-6x with what they had left behind on the device
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--workload", "serving",
+                            "--serving-rates", "400", "--serving-seconds", "5", "--serving-pool", "64"],
+                           capture_output=True, text=True, timeout=900)
+        lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+        if r.returncode != 0 or not lines:
+            raise RuntimeError(f"serving run exited {r.returncode}: {(r.stderr or r.stdout)[-400:]}")
+        sv = json.loads(lines[-1])["detail"]
         out["serving"] = sv
         ok = [r for r in sv["rates"] if r["failed"] == 0]
         if ok:
@@ -303,7 +312,8 @@ def run_workload(args, torch, world, rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
                 "config": {"workload": r["workload"], "l2": r["l2"]}, "detail": r}
     else:
-        r = wl.serving(torch, rates=(100, 200, 400, 800, 1600), duration_s=4.0, pool_size=128)
+        r = wl.serving(torch, rates=tuple(int(x) for x in args.serving_rates.split(",")),
+                       duration_s=args.serving_seconds, pool_size=args.serving_pool)
         best = max(r["rates"], key=lambda x: x["keys_per_s"])
         line = {"metric": "serving throughput (keys/s) with p50/p99 latency",
                 "value": best["keys_per_s"] / 1e9, "unit": "Gkeys/s", "n_gpus": 1,
@@ -332,6 +342,9 @@ def main():
     ap.add_argument("--segments", type=int, default=65536, help="batched: number of arrays")
     ap.add_argument("--max-len", type=int, default=1 << 20, help="batched: longest array")
     ap.add_argument("--loop-steps", type=int, default=2, help="batched: timed runs of the plain-sort loop")
+    ap.add_argument("--serving-rates", default="100,200,400,800,1600", help="serving: offered rates (req/s)")
+    ap.add_argument("--serving-seconds", type=float, default=4.0, help="serving: seconds per rate")
+    ap.add_argument("--serving-pool", type=int, default=128, help="serving: distinct requests")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -386,7 +399,12 @@ def main():
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = ClockSampler(local)
-    og.profile_enable(True)
+    # per-kernel CUDA events on every PROFILE_EVERY-th launch of each kernel:
+    # an event pair between two kernels stops the second from starting while
+    # the first drains (programmatic dependent launch), so bracketing every
+    # launch slowed the timed sort by 3 %; 15 and 7 are coprime, so over the
+    # timed steps every merge level is sampled
+    og.profile_enable(True, every=PROFILE_EVERY)
     launches0 = og.launch_count()
     if dist:
         dist.barrier()
@@ -401,6 +419,7 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     launches = og.launch_count() - launches0
+    detail = og.profile_detail()
     report = og.profile_report()
     og.profile_enable(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -472,12 +491,14 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
                      "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+                     "launches_timed": detail[dom_name][1],
                      "traffic": traffic,
                      "pipeline_frac": (2 * n * item * passes / (ms_step / 1e3) / 1e9) / peak,
                      # one read + write of the array at peak (P = 1), and all passes
                      "pass_floor_ms": 2 * n * item / (peak * 1e9) * 1e3,
                      "passes_floor_ms": 2 * n * item * passes / (peak * 1e9) * 1e3},
-        "kernels": {k: {"launches": c, "ms": ms} for k, (c, ms) in report.items()},
+        "kernels": {k: {"launches": c, "timed": t, "ms_per_launch": (ms / t if t else None)}
+                    for k, (c, t, ms) in detail.items()},
         "gpu_launches": launches,
         "tuning": tuning,
         "correct": ok,

@@ -193,10 +193,15 @@ int origami_partition_device(int kind, void* const* L, void* const* R, unsigned 
 
 /*
  * Launch accounting and profiling. Every kernel the library launches is
- * counted. While profiling is enabled each launch is also bracketed by two CUDA
- * events on its own stream; origami_profile_report() waits for them and writes
- * one "kernel,launches,total_ms" line per kernel into buf (returns the length,
- * or a negative status). Enabling (or disabling) clears earlier records.
+ * counted. While profiling is enabled launches are also bracketed by two CUDA
+ * events on their own stream: every launch for on = 1, every on-th launch of
+ * each kernel for on > 1 (the events sit between kernels that otherwise
+ * overlap their start-up with their predecessor's end, so timing fewer of them
+ * disturbs the timeline less); 0 disables. origami_profile_report() waits for
+ * the events and writes one "kernel,launches,timed_ms,timed" line per kernel
+ * into buf: all launches since enabling, and the total device milliseconds of
+ * the `timed` launches among them (returns the length, or a negative status).
+ * Enabling (or disabling) clears earlier records.
  */
 int origami_profile_enable(int on);
 int origami_profile_report(char* buf, uint64_t cap);

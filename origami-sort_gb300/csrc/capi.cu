@@ -29,6 +29,8 @@ struct ProfRec {
 };
 std::vector<ProfRec> g_recs;
 std::vector<cudaEvent_t> g_event_pool;
+std::map<std::string, uint64_t> g_prof_seen;  // launches per kernel since profiling was enabled
+uint32_t g_prof_every = 1;                     // time every k-th launch of each kernel
 
 cudaEvent_t take_event() {
     if (!g_event_pool.empty()) {
@@ -55,6 +57,10 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int prof_begin(const char* name, cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
+    uint64_t& seen = g_prof_seen[name];
+    const bool timed = seen % g_prof_every == 0;
+    ++seen;
+    if (!timed) return -1;
     ProfRec r{name, take_event(), take_event()};
     cudaEventRecord(r.a, st);
     g_recs.push_back(r);
@@ -940,12 +946,15 @@ uint64_t origami_arena_bytes_in_use(void) {
 }
 
 int origami_profile_enable(int on) {
+    if (on < 0) return fail(ORIGAMI_ERR_INVALID, "profile_enable: negative argument");
     std::lock_guard<std::mutex> lk(g_prof_mu);
     for (auto& r : g_recs) {
         g_event_pool.push_back(r.a);
         g_event_pool.push_back(r.b);
     }
     g_recs.clear();
+    g_prof_seen.clear();
+    g_prof_every = on > 1 ? (uint32_t)on : 1u;
     g_prof_on.store(on != 0);
     return ORIGAMI_OK;
 }
@@ -953,7 +962,7 @@ int origami_profile_enable(int on) {
 int origami_profile_report(char* buf, uint64_t cap) {
     if (!buf || cap == 0) return fail(ORIGAMI_ERR_INVALID, "report buffer is NULL");
     std::lock_guard<std::mutex> lk(g_prof_mu);
-    std::map<std::string, std::pair<uint64_t, double>> agg;
+    std::map<std::string, std::pair<uint64_t, double>> agg;  // timed launches, their total ms
     for (auto& r : g_recs) {
         CK(cudaEventSynchronize(r.b), "profile sync");
         float ms = 0.f;
@@ -964,9 +973,12 @@ int origami_profile_report(char* buf, uint64_t cap) {
     }
     std::string out;
     char line[256];
-    for (auto& kv : agg) {
-        snprintf(line, sizeof line, "%s,%llu,%.6f\n", kv.first.c_str(),
-                 (unsigned long long)kv.second.first, kv.second.second);
+    for (auto& kv : g_prof_seen) {
+        const auto it = agg.find(kv.first);
+        const uint64_t timed = it == agg.end() ? 0 : it->second.first;
+        const double ms = it == agg.end() ? 0.0 : it->second.second;
+        snprintf(line, sizeof line, "%s,%llu,%.6f,%llu\n", kv.first.c_str(), (unsigned long long)kv.second, ms,
+                 (unsigned long long)timed);
         out += line;
     }
     if (out.size() + 1 > cap) return fail(ORIGAMI_ERR_INVALID, "report buffer too small");

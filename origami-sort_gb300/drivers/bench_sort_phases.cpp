@@ -32,6 +32,8 @@ struct Result {
     std::string kernels;
 };
 
+// {kernel: (launches, total ms)} from origami_profile_report's
+// "kernel,launches,timed_ms,timed" lines (every launch is timed here).
 std::map<std::string, std::pair<long, double>> report() {
     std::vector<char> buf(1 << 16);
     std::map<std::string, std::pair<long, double>> m;
@@ -40,9 +42,13 @@ std::map<std::string, std::pair<long, double>> report() {
     std::istringstream in(std::string(buf.data(), (size_t)len));
     std::string line;
     while (std::getline(in, line)) {
-        const size_t a = line.rfind(','), b = line.rfind(',', a - 1);
-        if (a == std::string::npos || b == std::string::npos) continue;
-        m[line.substr(0, b)] = {std::stol(line.substr(b + 1, a - b - 1)), std::stod(line.substr(a + 1))};
+        const size_t c3 = line.rfind(',');
+        if (c3 == std::string::npos || c3 == 0) continue;
+        const size_t c2 = line.rfind(',', c3 - 1);
+        if (c2 == std::string::npos || c2 == 0) continue;
+        const size_t c1 = line.rfind(',', c2 - 1);
+        if (c1 == std::string::npos) continue;
+        m[line.substr(0, c1)] = {std::stol(line.substr(c1 + 1, c2 - c1 - 1)), std::stod(line.substr(c2 + 1, c3 - c2 - 1))};
     }
     return m;
 }

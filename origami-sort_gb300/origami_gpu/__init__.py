@@ -460,21 +460,29 @@ def partition_ptrs(streams, guesses, kind):
     return [int(x) for x in partition(streams, [int(sum(guesses))], kind)[0]]
 
 
-def profile_enable(on=True):
-    check(lib().origami_profile_enable(1 if on else 0))
+def profile_enable(on=True, every=1):
+    """Time kernel launches with CUDA events: every launch, or every `every`-th
+    launch of each kernel (on=False switches timing off)."""
+    check(lib().origami_profile_enable(max(1, int(every)) if on else 0))
 
 
-def profile_report():
-    """{kernel: (launches, total_ms)} for the launches since profile_enable()."""
+def profile_detail():
+    """{kernel: (launches, timed, timed_ms)} for the launches since profile_enable()."""
     buf = ctypes.create_string_buffer(1 << 16)
     rc = lib().origami_profile_report(buf, len(buf))
     if rc < 0:
         check(rc)
     out = {}
     for line in buf.value.decode().splitlines():
-        name, cnt, ms = line.rsplit(",", 2)
-        out[name] = (int(cnt), float(ms))
+        name, cnt, ms, timed = line.rsplit(",", 3)
+        out[name] = (int(cnt), int(timed), float(ms))
     return out
+
+
+def profile_report():
+    """{kernel: (launches, total_ms)} for the launches since profile_enable();
+    with sampled timing, total_ms is the timed launches' mean times `launches`."""
+    return {k: (c, ms * c / t if t else 0.0) for k, (c, t, ms) in profile_detail().items()}
 
 
 def launch_count():

@@ -177,3 +177,12 @@ def test_segmented_tuning_in_the_tuning_file(lib, tmp_path):
     og.tuning_load(path)
     assert og.seg_tuning_get(og.KV64, 1 << 16, 1) == 1
     og.seg_tuning_set(og.KV64, 1 << 22, 1 << 6, 0)
+
+
+def test_profile_switch(lib):
+    # host-side bookkeeping only: nothing is launched, so the report is empty
+    assert lib.origami_profile_enable(-1) == og.ERR_INVALID
+    og.profile_enable(True, every=7)
+    assert og.profile_detail() == {}
+    og.profile_enable(False)
+    assert og.profile_report() == {}
