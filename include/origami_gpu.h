@@ -326,11 +326,11 @@ int origami_generate_device(int kind, void* d, uint64_t n, int dist, uint64_t se
  * config.h constants and the bench_sort_phases switch-point sweeps). Every
  * sort with min_k = 0 takes its pass shape from a table indexed by item kind
  * and size class floor(log2 n): the merge fan-in (2 = binary passes, 4/8/16 =
- * k-way passes) and, for binary passes, one of three merge shapes: 0 (the
+ * k-way passes) and, for binary passes, one of four merge shapes: 0 (the
  * default) and 1 are two tile shapes (threads, items per thread, tile) of the
  * persistent bulk-copy merge kernel where the item kind has one, 2 is shape 0
  * as one tile per CTA, which interleaves better with sorts running on other
- * streams. min_k = 2 keeps the table's merge shape with binary passes; larger
+ * streams, 3 is shape 0's tile with half the items per thread. min_k = 2 keeps the table's merge shape with binary passes; larger
  * min_k forces that fan-in.
  *   origami_autotune   times every shape on n generated device items and stores
  *                      the fastest for n's size class; `report` (may be NULL)

@@ -652,7 +652,7 @@ int tune_load_file(const char* path) {
         if (std::sscanf(line, "%d %d %d %d", &kind, &cls, &fan, &var) != 4) continue;
         if (kind < 0 || kind > 4 || cls < 0 || cls >= TUNE_CLASSES) continue;
         if (fan != 2 && fan != 4 && fan != 8 && fan != 16) continue;
-        if (var < 0 || var > 2 || (fan != 2 && var != 0)) continue;
+        if (var < 0 || var > 3 || (fan != 2 && var != 0)) continue;
         g_tune[kind][cls].store(shape_code(fan, var), std::memory_order_relaxed);
         ++loaded;
     }
@@ -1007,8 +1007,8 @@ int origami_tuning_get(int kind, uint64_t n, int* fan, int* variant) {
 int origami_tuning_set(int kind, uint64_t n, int fan, int variant) {
     if (!valid_kind(kind)) return fail(ORIGAMI_ERR_DTYPE, "unknown item kind %d", kind);
     if (fan != 2 && fan != 4 && fan != 8 && fan != 16) return fail(ORIGAMI_ERR_INVALID, "fan must be 2, 4, 8 or 16");
-    if (variant < 0 || variant > 2 || (fan != 2 && variant != 0))
-        return fail(ORIGAMI_ERR_INVALID, "variant must be 0, 1 or 2 (1 and 2 only with fan 2)");
+    if (variant < 0 || variant > 3 || (fan != 2 && variant != 0))
+        return fail(ORIGAMI_ERR_INVALID, "variant must be 0 to 3 (1 to 3 only with fan 2)");
     std::call_once(g_tune_once, tune_init);
     g_tune[kind][size_class(n)].store(shape_code(fan, variant), std::memory_order_relaxed);
     return ORIGAMI_OK;
@@ -1055,8 +1055,8 @@ int origami_autotune(int kind, uint64_t n, char* report, uint64_t cap) {
     CK(cudaMallocAsync(&p, bytes, st), "autotune buffers");
     cudaError_t e = cudaMallocAsync(&d, bytes, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&t, bytes, st);
-    const int codes[] = {shape_code(2, 0), shape_code(2, 1), shape_code(2, 2), shape_code(4, 0), shape_code(8, 0),
-                         shape_code(16, 0)};
+    const int codes[] = {shape_code(2, 0), shape_code(2, 1), shape_code(2, 2), shape_code(2, 3),
+                         shape_code(4, 0), shape_code(8, 0), shape_code(16, 0)};
     uint64_t wbytes = 0;
     for (int c : codes) wbytes = std::max<uint64_t>(wbytes, scratch_bytes(kind, n, 0, c));
     if (e == cudaSuccess) e = cudaMallocAsync(&work, wbytes, st);

@@ -36,6 +36,8 @@ struct Config<uint32_t> {
     static constexpr int P2_NT = 288, P2_VT = 32, P2_TILE = 8192, P2_MINB = 3;  // second tile shape
     static constexpr bool P2_BULK = true;
     static constexpr int PI_MINB = 1;  // the first shape as one tile per CTA (variant 2)
+    // variant 3: the first shape's tile with half the keys per thread
+    static constexpr int P3_NT = 288, P3_VT = 16, P3_MINB = 4;
     static constexpr bool STABLE = false;
 };
 template <>
@@ -49,6 +51,7 @@ struct Config<uint64_t> {
     static constexpr int P2_NT = 288, P2_VT = 16, P2_TILE = 4096, P2_MINB = 3;
     static constexpr bool P2_BULK = true;
     static constexpr int PI_MINB = 8;
+    static constexpr int P3_NT = 320, P3_VT = 8, P3_MINB = 3;
     static constexpr bool STABLE = false;
 };
 template <>
@@ -62,6 +65,7 @@ struct Config<KV64> {
     static constexpr int P2_NT = 192, P2_VT = 11, P2_TILE = 2048, P2_MINB = 3;
     static constexpr bool P2_BULK = true;
     static constexpr int PI_MINB = 1;
+    static constexpr int P3_NT = 160, P3_VT = 7, P3_MINB = 5;  // serial blocks of 7
     static constexpr bool STABLE = true;
 };
 
@@ -157,6 +161,10 @@ using PairMerge2 =
 // overlap another's merges (a persistent kernel holds the SMs until it drains).
 template <class T>
 using PairMergeI = PairMerge<T, Config<T>::P_NT, Config<T>::P_VT, Config<T>::P_TILE, Config<T>::PI_MINB, false>;
+// The first shape's tile merged with half the items per thread (more threads,
+// fewer registers each): the autotuner's choice of items per thread.
+template <class T>
+using PairMerge3 = PairMerge<T, Config<T>::P3_NT, Config<T>::P3_VT, Config<T>::P_TILE, Config<T>::P3_MINB, true>;
 
 // Resident CTAs of the k-way merge kernel on the whole GPU (its persistent grid).
 template <class T>
@@ -367,6 +375,7 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
         PairMerge1<T>::configure();
         PairMerge2<T>::configure();
         PairMergeI<T>::configure();
+        PairMerge3<T>::configure();
         cudaFuncSetAttribute(range_merge_kernel<T, RunLists<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)KwayLayout<T>::SMEM);
         cudaFuncSetAttribute(kb_cut_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -448,6 +457,8 @@ cudaError_t sort_pipeline_io(const T* in, T* out, T* wa, T* wb, uint64_t n, uint
                     PairMerge2<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
                 else if (variant == 2)
                     PairMergeI<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
+                else if (variant == 3)
+                    PairMerge3<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
                 else
                     PairMerge1<T>::launch(cur, nxt, n, run, splits, tiles, xo, claim, err, st);
             });

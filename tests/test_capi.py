@@ -116,9 +116,11 @@ def test_tuning_table_roundtrip(lib, tmp_path):
     with pytest.raises(og.OrigamiError):
         og.tuning_set(og.U32, 100, 4, 1)  # the tile shape choice is for binary passes
     with pytest.raises(og.OrigamiError):
-        og.tuning_set(og.U32, 100, 2, 3)
+        og.tuning_set(og.U32, 100, 2, 4)
     og.tuning_set(og.U64, 1 << 24, 2, 2)  # one tile per CTA
     assert og.tuning_get(og.U64, 1 << 24) == (2, 2)
+    og.tuning_set(og.U64, 1 << 24, 2, 3)  # half the items per thread
+    assert og.tuning_get(og.U64, 1 << 24) == (2, 3)
     og.tuning_set(og.U64, 1 << 24, 2, 0)
     og.tuning_set(og.U32, 1 << 20, 2, 0)
     og.tuning_set(og.KV64, 1 << 27, 2, 0)

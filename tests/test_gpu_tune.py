@@ -40,7 +40,7 @@ def expected(a):
     return a[np.argsort(orc.keys_of(a), kind="stable")]
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3])
 @pytest.mark.parametrize("kind", [og.U32, og.U64, og.I64, og.KV64, og.KVU64])
 @pytest.mark.parametrize("n", [5000, 300_007, (1 << 22) + 9])
 def test_merge_shape_parity(kind, n, variant):
@@ -69,8 +69,8 @@ def test_autotune_chooses_and_sorts(kind):
     try:
         r = og.autotune(kind, n)
         lines = [l for l in r["report"].splitlines() if l.startswith("fan=")]
-        assert len(lines) == 6  # three binary merge shapes, fan-in 4, 8 and 16
-        assert r["fan"] in (2, 4, 8, 16) and r["variant"] in (0, 1, 2)
+        assert len(lines) == 7  # four binary merge shapes, fan-in 4, 8 and 16
+        assert r["fan"] in (2, 4, 8, 16) and r["variant"] in (0, 1, 2, 3)
         assert og.tuning_get(kind, n) == (r["fan"], r["variant"])
         a = make(kind, n, seed=1)
         d = torch.from_numpy(a.view(np.uint8).copy()).cuda()
@@ -81,7 +81,7 @@ def test_autotune_chooses_and_sorts(kind):
         og.tuning_set(kind, n, *prev)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("kind", [og.U32, og.KV64])
 def test_concurrent_streams(kind, variant):
     # sorts on four streams at once: the persistent merge kernels of one sort
