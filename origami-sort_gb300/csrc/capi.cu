@@ -510,13 +510,12 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
         p.total = 2 * p.data + p.ws;
         return p;
     }
-    // chunks sort on HOST_LANES-1 streams at once; binary passes use the
-    // one-tile-per-CTA merge shape, whose launches from the different streams
-    // interleave (one chunk's splitter searches overlap another's merges; 8
-    // chunk sorts of 2^25 keys: 6.97 ms on 4 streams against 8.3 ms for the
-    // persistent kernels on one)
-    p.cfan = shape_for(kind, p.chunk_n, min_k);  // the chunks' own tuned shape
-    if (shape_fan(p.cfan) == 2) p.cfan = shape_code(2, 2);
+    // chunks sort on HOST_LANES-1 streams at once, with binary passes of the
+    // one-tile-per-CTA merge shape (unless the caller forces a fan-in), whose
+    // launches from the different streams interleave (one chunk's splitter
+    // searches overlap another's merges; 8 chunk sorts of 2^25 keys: 6.97 ms
+    // on 4 streams against 8.3 ms for the persistent kernels on one)
+    p.cfan = min_k > 2 ? shape_code(fan_of(min_k), 0) : shape_code(2, 2);
     p.ws = a256(typed_scratch_io(kind, p.chunk_n, 0, p.cfan, 0));
     // the merges across chunks are one k-way pass: bound by the host link it
     // writes (1 GiB in ~5.6 ms), which hides its cost per level
@@ -660,9 +659,33 @@ int tune_load_file(const char* path) {
     return loaded;
 }
 
+// Built-in pass shapes: the autotuner's choice on one GB300 (two sweeps, the
+// same winner in both, ahead of binary passes with the first tile shape by at
+// least 1.5 %), for size classes floor(log2 n). Every other class keeps binary
+// passes with the first tile shape. Signed kinds share their unsigned kind's
+// kernels and entries. The sampled 16-way pass wins where the data is about
+// the size of L2 (u32 2^25 keys: 1.00 against 1.02 ms; key-value 2^23 pairs:
+// 0.91 against 0.95 ms).
+struct TuneDefault {
+    int kind, cls, fan, variant;
+};
+constexpr TuneDefault kTuneDefaults[] = {
+    {ORIGAMI_U32, 18, 16, 0},  {ORIGAMI_U32, 19, 2, 3},   {ORIGAMI_U32, 20, 2, 3},   {ORIGAMI_U32, 21, 16, 0},
+    {ORIGAMI_U32, 22, 2, 3},   {ORIGAMI_U32, 23, 2, 2},   {ORIGAMI_U32, 25, 16, 0},  {ORIGAMI_U64, 17, 16, 0},
+    {ORIGAMI_U64, 18, 2, 3},   {ORIGAMI_U64, 19, 2, 3},   {ORIGAMI_U64, 20, 16, 0},  {ORIGAMI_U64, 21, 2, 2},
+    {ORIGAMI_U64, 22, 2, 2},   {ORIGAMI_U64, 23, 2, 1},   {ORIGAMI_KV64, 17, 2, 3},  {ORIGAMI_KV64, 19, 16, 0},
+    {ORIGAMI_KV64, 20, 16, 0}, {ORIGAMI_KV64, 22, 16, 0}, {ORIGAMI_KV64, 23, 16, 0}, {ORIGAMI_KV64, 24, 2, 1},
+    {ORIGAMI_KV64, 25, 2, 1},  {ORIGAMI_KV64, 26, 2, 1},
+};
+
 void tune_init() {
     for (auto& row : g_tune)
         for (auto& c : row) c.store(shape_code(2, 0), std::memory_order_relaxed);
+    for (const TuneDefault& t : kTuneDefaults) {
+        g_tune[t.kind][t.cls].store(shape_code(t.fan, t.variant), std::memory_order_relaxed);
+        const int twin = t.kind == ORIGAMI_U64 ? ORIGAMI_I64 : (t.kind == ORIGAMI_KV64 ? ORIGAMI_KVU64 : -1);
+        if (twin >= 0) g_tune[twin][t.cls].store(shape_code(t.fan, t.variant), std::memory_order_relaxed);
+    }
     for (auto& row : g_seg_tune)
         for (auto& c : row) c.store(0, std::memory_order_relaxed);
     if (const char* path = std::getenv("ORIGAMI_TUNING")) tune_load_file(path);

@@ -98,11 +98,16 @@ def test_server_without_device(lib):
 def test_tuning_table_roundtrip(lib, tmp_path):
     # the table needs no device: set, read back, save, reset, load
     for k in range(5):
-        assert og.tuning_get(k, 1 << 20) == (2, 0)  # default: binary passes, first tile shape
+        assert og.tuning_get(k, 1 << 28) == (2, 0)  # default: binary passes, first tile shape
+    # built-in entries: the 16-way k-way pass where the data is about L2-sized
+    assert og.tuning_get(og.U32, 1 << 25) == (16, 0)
+    assert og.tuning_get(og.KV64, 1 << 23) == og.tuning_get(og.KVU64, 1 << 23) == (16, 0)
+    assert og.tuning_get(og.U64, 1 << 21) == og.tuning_get(og.I64, 1 << 21) == (2, 2)
+    built_in = og.tuning_get(og.U32, 1 << 20)
     og.tuning_set(og.U32, 1 << 20, 2, 1)
     og.tuning_set(og.KV64, 1 << 27, 8, 0)
     assert og.tuning_get(og.U32, (1 << 21) - 1) == (2, 1)  # same size class
-    assert og.tuning_get(og.U32, 1 << 21) == (2, 0)
+    assert og.tuning_get(og.U32, 1 << 21) == (16, 0)  # the next class keeps its own entry
     path = tmp_path / "tune.txt"
     og.tuning_save(path)
     lines = sorted(path.read_text().split("\n"))
@@ -122,7 +127,7 @@ def test_tuning_table_roundtrip(lib, tmp_path):
     og.tuning_set(og.U64, 1 << 24, 2, 3)  # half the items per thread
     assert og.tuning_get(og.U64, 1 << 24) == (2, 3)
     og.tuning_set(og.U64, 1 << 24, 2, 0)
-    og.tuning_set(og.U32, 1 << 20, 2, 0)
+    og.tuning_set(og.U32, 1 << 20, *built_in)
     og.tuning_set(og.KV64, 1 << 27, 2, 0)
 
 
