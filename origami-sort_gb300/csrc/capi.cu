@@ -510,12 +510,13 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
         p.total = 2 * p.data + p.ws;
         return p;
     }
-    // chunks sort on HOST_LANES-1 streams at once, with binary passes of the
-    // one-tile-per-CTA merge shape (unless the caller forces a fan-in), whose
-    // launches from the different streams interleave (one chunk's splitter
-    // searches overlap another's merges; 8 chunk sorts of 2^25 keys: 6.97 ms
-    // on 4 streams against 8.3 ms for the persistent kernels on one)
-    p.cfan = min_k > 2 ? shape_code(fan_of(min_k), 0) : shape_code(2, 2);
+    // chunks sort on HOST_LANES-1 streams at once: by default with 16-way
+    // passes (a 1 GiB u32 call from pinned memory: 14.03 ms per call, against
+    // 14.35 with binary passes of the one-tile-per-CTA shape, whose launches
+    // from the different streams interleave, 14.46 with the persistent binary
+    // kernel and 14.27 with 8-way passes); min_k = 2 keeps binary passes of the
+    // interleaving shape, larger min_k that fan-in
+    p.cfan = min_k > 2 ? shape_code(fan_of(min_k), 0) : (min_k == 2 ? shape_code(2, 2) : shape_code(16, 0));
     p.ws = a256(typed_scratch_io(kind, p.chunk_n, 0, p.cfan, 0));
     // the merges across chunks are one k-way pass: bound by the host link it
     // writes (1 GiB in ~5.6 ms), which hides its cost per level
