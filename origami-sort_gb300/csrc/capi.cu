@@ -738,7 +738,11 @@ int sort_host_impl(int kind, void* d, void* tmp, uint64_t n, uint64_t sort_n, un
 }  // namespace
 
 namespace origami {
-uint64_t host_pipe_bytes(int kind, uint64_t n) { return host_pipe_plan(kind, n, 0, 0).total; }
+// The serving loop's large requests: the pipelined host sort with binary
+// passes of the interleaving shape for the chunks (min_k = 2), because the
+// loop's other batches run beside it; persistent 16-way chunk sorts hold
+// every SM while they run (400 requests/s: p50 0.35 -> 3.6 ms, p99 14 -> 108 ms).
+uint64_t host_pipe_bytes(int kind, uint64_t n) { return host_pipe_plan(kind, n, 0, 2).total; }
 
 int host_pipe_sort(int kind, const void* in, void* out, uint64_t n, void* block, cudaStream_t st) {
     auto view = [](const void* p) -> void* {
@@ -749,7 +753,7 @@ int host_pipe_sort(int kind, const void* in, void* out, uint64_t n, void* block,
     void* vout = view(out);
     if (!vin || !vout || ((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
         return fail(ORIGAMI_ERR_INVALID, "buffers the device cannot address directly");
-    return host_pipe_run(kind, const_cast<void*>(in), out, vin, vout, n, 0, host_pipe_plan(kind, n, 0, 0), block, st);
+    return host_pipe_run(kind, const_cast<void*>(in), out, vin, vout, n, 0, host_pipe_plan(kind, n, 0, 2), block, st);
 }
 
 int noalloc_fail(int code, const char* msg) { return fail(code, "%s", msg); }
