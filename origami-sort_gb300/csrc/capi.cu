@@ -676,7 +676,7 @@ constexpr TuneDefault kTuneDefaults[] = {
     {ORIGAMI_U64, 18, 2, 3},   {ORIGAMI_U64, 19, 2, 3},   {ORIGAMI_U64, 20, 16, 0},  {ORIGAMI_U64, 21, 2, 2},
     {ORIGAMI_U64, 22, 2, 2},   {ORIGAMI_U64, 23, 2, 1},   {ORIGAMI_KV64, 17, 2, 3},  {ORIGAMI_KV64, 19, 16, 0},
     {ORIGAMI_KV64, 20, 16, 0}, {ORIGAMI_KV64, 22, 16, 0}, {ORIGAMI_KV64, 23, 16, 0}, {ORIGAMI_KV64, 24, 2, 1},
-    {ORIGAMI_KV64, 25, 2, 1},  {ORIGAMI_KV64, 26, 2, 1},
+    {ORIGAMI_KV64, 25, 2, 1},  {ORIGAMI_KV64, 26, 2, 1},   {ORIGAMI_KV64, 27, 2, 1},   {ORIGAMI_KV64, 28, 2, 1},
 };
 
 void tune_init() {
