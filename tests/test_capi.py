@@ -105,6 +105,7 @@ def test_tuning_table_roundtrip(lib, tmp_path):
     assert og.tuning_get(og.U64, 1 << 21) == og.tuning_get(og.I64, 1 << 21) == (2, 2)
     assert og.tuning_get(og.KV64, 1 << 28) == og.tuning_get(og.KVU64, 1 << 28) == (2, 1)
     built_in = og.tuning_get(og.U32, 1 << 20)
+    built_in_kv = og.tuning_get(og.KV64, 1 << 27)
     og.tuning_set(og.U32, 1 << 20, 2, 1)
     og.tuning_set(og.KV64, 1 << 27, 8, 0)
     assert og.tuning_get(og.U32, (1 << 21) - 1) == (2, 1)  # same size class
@@ -129,7 +130,7 @@ def test_tuning_table_roundtrip(lib, tmp_path):
     assert og.tuning_get(og.U64, 1 << 24) == (2, 3)
     og.tuning_set(og.U64, 1 << 24, 2, 0)
     og.tuning_set(og.U32, 1 << 20, *built_in)
-    og.tuning_set(og.KV64, 1 << 27, 2, 0)
+    og.tuning_set(og.KV64, 1 << 27, *built_in_kv)
 
 
 def test_noalloc_rejects_bad_arguments_on_the_host(lib):
