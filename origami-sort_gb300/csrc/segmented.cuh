@@ -343,6 +343,21 @@ __global__ void __launch_bounds__(SegShape<T>::NTM, SegCfg<T>::TILE_MINB) seg_ti
         const uint32_t t = j - st.cnt[s];
         const uint64_t p0 = st.off[s] + (uint64_t)t * C::TILE;
         const int cnt = (int)min((uint64_t)C::TILE, g.len - (uint64_t)t * C::TILE);
+        if (threadIdx.x == 32 && j + gridDim.x < total) {
+            // this CTA's next tile into L2 while this one sorts: the whole
+            // 16-byte chunks inside it (and inside the buffer)
+            const uint32_t jn = j + gridDim.x, sn = st.tileseg[jn];
+            const SegGeom<T> gn(st.off, sn, st.n);
+            constexpr uint64_t IB = sizeof(T), TL = C::TILE;
+            const uint64_t tn = jn - st.cnt[sn];
+            const uint64_t items = gn.len > tn * TL ? gn.len - tn * TL : 0;
+            const uint64_t b0 = (st.off[sn] + tn * TL) * IB;
+            const uint64_t lim = (st.n * IB) & ~15ull;
+            const uint64_t b1 = b0 + (items < TL ? items : TL) * IB;
+            const uint64_t c0 = (b0 + 15) & ~15ull, c1 = (b1 < lim ? b1 : lim) & ~15ull;
+            if (items > 0 && c1 > c0)
+                bulk_prefetch_l2(reinterpret_cast<const char*>(d) + c0, (uint32_t)(c1 - c0));
+        }
         if (!seg_tile_sort<T>(d, seg_buf<T>(g.levels, 0, d, tmp), p0, cnt, xmask, g.levels == 0 ? xmask : 0,
                               smem_raw, split, &bar, phase, st.err, st.spin))
             return;
