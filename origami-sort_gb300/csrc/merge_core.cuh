@@ -231,31 +231,9 @@ __device__ __forceinline__ void merge_round_lists(const T* src, T* dst, const in
     __syncthreads();
 }
 
-// Round over a single pair whose parts sit anywhere in `src` (A = [as, as+na),
-// B = [bs, bs+nb)); the merged output goes to dst[0 .. na+nb). `split` is
-// shared scratch of (na+nb)/VO + 2 ints.
-template <class T, int NT, int VT, bool STABLE>
-__device__ __forceinline__ void merge_pair_round(const T* src, int as, int na, int bs, int nb, T* dst,
-                                                 int* split) {
-    constexpr int VO = Block<T, VT, STABLE>::VO;
-    const int tid = threadIdx.x;
-    const int total = na + nb;
-    const int nblk = (total + VO - 1) / VO;
-    for (int blk = tid; blk < nblk; blk += NT)
-        split[blk] = merge_path_ix<T, LinIdx>(src, as, na, bs, nb, blk * VO);
-    __syncthreads();
-    for (int blk = tid; blk < nblk; blk += NT) {
-        const int diag = blk * VO;
-        const int cnt = min(VO, total - diag);
-        const int sa = split[blk];
-        const int ea = (blk + 1 < nblk) ? split[blk + 1] : na;
-        merge_block<T, VT, STABLE, LinIdx>(src, dst, as + sa, bs + (diag - sa), ea - sa, cnt, diag);
-    }
-    __syncthreads();
-}
-
-// merge_pair_round that writes its output over its own input: `buf` holds A
-// at [as, as+na) and B at [bs, bs+nb) and receives the merge at [0, na+nb).
+// One merge round over a single pair that writes its output over its own
+// input: `buf` holds A at [as, as+na) and B at [bs, bs+nb) and receives the
+// merge at [0, na+nb).
 // Every thread owns at most one block (NT * VO >= na + nb), keeps it in
 // registers while the others read, then stores it. The output may therefore
 // share the input's shared memory, which halves the footprint of a tile.
