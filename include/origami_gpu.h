@@ -330,13 +330,17 @@ int origami_generate_device(int kind, void* d, uint64_t n, int dist, uint64_t se
  * default) and 1 are two tile shapes (threads, items per thread, tile) of the
  * persistent bulk-copy merge kernel where the item kind has one, 2 is shape 0
  * as one tile per CTA, which interleaves better with sorts running on other
- * streams, 3 is shape 0's tile with half the items per thread. min_k = 2 keeps the table's merge shape with binary passes; larger
- * min_k forces that fan-in.
+ * streams, 3 is shape 0's tile with half the items per thread. The table
+ * starts from built-in entries measured on a GB300 (16-way passes for some
+ * sizes about as large as L2, other binary shapes for others; binary passes
+ * with shape 0 elsewhere). min_k = 2 keeps the table's merge shape with
+ * binary passes; larger min_k forces that fan-in.
  *   origami_autotune   times every shape on n generated device items and stores
  *                      the fastest for n's size class; `report` (may be NULL)
  *                      receives one "fan= variant= ms=" line per shape.
  *   get / set          read or write one entry.
- *   save / load        the non-default entries as "kind class fan variant"
+ *   save / load        the entries other than binary passes with shape 0 as
+ *                      "kind class fan variant"
  *                      lines, and the segmented table's (below) as
  *                      "seg kind class shape" lines. The file named by
  *                      ORIGAMI_TUNING, if set, is loaded at first use.
