@@ -432,8 +432,8 @@ bool is_pinned(const void* p) {
 //  * Small sorts, fan-in > 2, or chunk sizes of at most one chunk: one
 //    pipeline whose first kernel reads the host input and whose last pass
 //    writes the host output, with the passes in between in two arena buffers.
-//  * Large sorts: the input is cut into chunks of chunk_n (a power of two,
-//    8 to 16 chunks). Each chunk arrives in HBM (a copy-engine transfer for
+//  * Large sorts: the input is cut into chunks of chunk_n (a power of two of
+//    at least 2^22 items; 4 to 16 chunks, more than 8 above 2^26 items). Each chunk arrives in HBM (a copy-engine transfer for
 //    pinned memory, else the first kernel's own reads) and is sorted on one of
 //    four compute streams while the next chunks are in flight; one k-way pass
 //    across the chunks follows, cut into output slices that go to pinned host
@@ -502,7 +502,14 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
     const uint64_t limit = (sort_n == 0 || sort_n >= n) ? n : sort_n;
     p.fan = shape_for(kind, n, min_k);
     p.chunk_n = 1ull << 22;
-    while (p.chunk_n * 16 <= n) p.chunk_n <<= 1;  // 8 to 16 chunks (4 and 16 measured slower at 1 GiB)
+    // at most 16 chunks, so that one k-way pass of fan-in 16 merges them, and
+    // more than 8 where the chunks are larger than the smallest size. The chunk sorts are bound by the GPU's sorting throughput,
+    // not by the link: the smaller the chunks, the earlier the first one
+    // arrives and the fewer levels the chunk sorts merge before the final pass,
+    // whose levels hide under its copies to the host (1 GiB u32 from pinned
+    // memory: 16 chunks 13.74 ms per call, 8 chunks 14.09 ms; the last chunk
+    // sort ends 7.40 against 7.86 ms after the first copy starts)
+    while (p.chunk_n * 16 < n) p.chunk_n <<= 1;
     p.chunked = n >= 4 * p.chunk_n && limit > p.chunk_n;
     p.data = a256(n * item_bytes(kind));
     if (!p.chunked) {

@@ -181,6 +181,10 @@ def test_pinned_host_buffers():
     (og.KV64, (1 << 24) + 3, False, 0),
     (og.U64, 1 << 24, True, 1 << 23),
     (og.KVU64, 1 << 24, True, 1 << 23),
+    # 16 chunks merged by one 16-way pass: into pinned output by slices, and
+    # into pageable output directly
+    (og.U32, 1 << 26, True, 0),
+    (og.U64, 1 << 26, False, 0),
 ])
 def test_host_chunked_pipeline(kind, n, pinned, sort_n):
     """Large host sorts: chunks sorted while the next ones arrive, then merged,
