@@ -433,11 +433,13 @@ bool is_pinned(const void* p) {
 //    pipeline whose first kernel reads the host input and whose last pass
 //    writes the host output, with the passes in between in two arena buffers.
 //  * Large sorts: the input is cut into chunks of chunk_n (a power of two of
-//    at least 2^22 items; 4 to 16 chunks, more than 8 above 2^26 items). Each chunk arrives in HBM (a copy-engine transfer for
-//    pinned memory, else the first kernel's own reads) and is sorted on one of
-//    four compute streams while the next chunks are in flight; one k-way pass
-//    across the chunks follows, cut into output slices that go to pinned host
-//    output while the next slices merge (or writing the host output directly).
+//    at least 2^22 items; 4 to 16 chunks, more than 8 above 2^26 items). Each
+//    chunk arrives in HBM (a copy-engine transfer for pinned memory, else the
+//    first kernel's own reads) and is sorted on one of four compute streams
+//    while the next chunks are in flight; one k-way pass across the chunks
+//    follows and writes the host output itself, or (the serving loop, pinned
+//    output) is cut into output slices that go to the host by copies while
+//    the next slices merge.
 //    The host link carries each byte once each way, overlapped with the sorts.
 cudaError_t typed_kway_final(int kind, const void* in, void* out, uint64_t n, uint64_t run, int fan, uint64_t xout,
                              void* scratch, cudaStream_t st, int slices, void (*cb)(void*, uint64_t, uint64_t),
@@ -490,6 +492,12 @@ struct SliceCopy {
 // device memory it takes from one block (each part 256-byte aligned).
 struct HostPipePlan {
     bool chunked = false;
+    // pinned output of a chunked sort: copies of finished output slices (the
+    // SMs stay free for other work while the link drains them), or the final
+    // pass writing the host buffer itself (ends sooner: 1 GiB u32 13.4 against
+    // 13.75 ms per call, as the first bytes leave without waiting for the
+    // slice boundaries and a first slice)
+    bool slice_copies = false;
     uint64_t chunk_n = 0;
     int fan = 0, cfan = 0, mfan = 0;
     uint64_t data = 0, ws = 0, wm = 0, total = 0;  // A and B (data each), lane scratch, merge scratch
@@ -541,10 +549,11 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
 // the result is in place. Large sorts are cut into chunks: each chunk arrives
 // in HBM (a copy-engine transfer for pinned memory, else the first kernel's
 // own reads) and is sorted on one of four streams while the next chunks are in
-// flight; the merge across chunks follows as one k-way pass, cut into output
-// slices that go to pinned host output while the next slices merge (or
-// writing the host output directly). Small sorts run one pipeline whose first
-// kernel reads the input and whose last pass writes the output.
+// flight; the merge across chunks follows as one k-way pass that writes the
+// host output (or, with plan.slice_copies and pinned output, is cut into
+// output slices copied to the host while the next slices merge). Small sorts
+// run one pipeline whose first kernel reads the input and whose last pass
+// writes the output.
 int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n, uint64_t sort_n,
                   const HostPipePlan& p, void* block, cudaStream_t st) {
     const uint64_t ib = item_bytes(kind);
@@ -600,7 +609,7 @@ int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void
         }
         if (e == cudaSuccess) {
             for (int i = 1; i < HOST_LANES - 1; ++i) cudaStreamWaitEvent(st, event_on(lanes[i]), 0);
-            if (limit == n && is_pinned(host_out)) {
+            if (limit == n && p.slice_copies && is_pinned(host_out)) {
                 // one k-way pass into HBM in 16 slices; each finished slice goes
                 // to the host on the copy stream while the next ones merge (at
                 // 1 GiB, 8 slices finish 0.1-0.2 ms later and 32 about 1 ms later)
@@ -760,7 +769,9 @@ int host_pipe_sort(int kind, const void* in, void* out, uint64_t n, void* block,
     void* vout = view(out);
     if (!vin || !vout || ((((uintptr_t)vin) | ((uintptr_t)vout)) & 15))
         return fail(ORIGAMI_ERR_INVALID, "buffers the device cannot address directly");
-    return host_pipe_run(kind, const_cast<void*>(in), out, vin, vout, n, 0, host_pipe_plan(kind, n, 0, 2), block, st);
+    HostPipePlan p = host_pipe_plan(kind, n, 0, 2);
+    p.slice_copies = true;  // the loop's other batches run beside this one
+    return host_pipe_run(kind, const_cast<void*>(in), out, vin, vout, n, 0, p, block, st);
 }
 
 int noalloc_fail(int code, const char* msg) { return fail(code, "%s", msg); }
