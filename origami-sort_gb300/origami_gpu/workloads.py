@@ -285,9 +285,15 @@ def serving(torch, rates=(100, 200, 400, 800), duration_s=3.0, pool_size=96, see
         for r in rates:
             st = serve_rate(s, pool, r, duration_s, seed + r)
             out["rates"].append({k: st[k] for k in fields})
-        # saturation: two rounds of the pool submitted back to back
-        st = serve_rate(s, pool, None, 0, seed, max_requests=2 * len(pool.items))
-        out["saturation"] = {k: st[k] for k in fields if k != "offered_rate"}
+        # saturation: two rounds of the pool submitted back to back, three
+        # times (one such run lasts about 0.1 s and varied by +-20 % between
+        # runs); keys/s over all three, latency and counts of the median run
+        runs = [serve_rate(s, pool, None, 0, seed + i, max_requests=2 * len(pool.items)) for i in range(3)]
+        med = sorted(runs, key=lambda r: r["keys_per_s"])[1]
+        out["saturation"] = {k: med[k] for k in fields if k != "offered_rate"}
+        secs = sum(r["keys"] / r["keys_per_s"] for r in runs if r["keys_per_s"] > 0)
+        out["saturation"]["keys_per_s"] = sum(r["keys"] for r in runs) / secs if secs > 0 else 0.0
+        out["saturation"]["keys_per_s_runs"] = [r["keys_per_s"] for r in runs]
     if check_results:
         bad = 0
         for it in pool.items:
@@ -300,16 +306,18 @@ def serving(torch, rates=(100, 200, 400, 800), duration_s=3.0, pool_size=96, see
                 k = h.numpy().view(np.uint64)[0::2]
             bad += int(not np.all(k[1:] >= k[:-1]))
         out["outputs_sorted"] = bad == 0
-    # the plain single-array sort called once per request, same requests
+    # the plain single-array sort called once per request, same requests,
+    # two rounds of the pool
     L = lib()
     res = ctypes.c_void_p()
     dt = 0.0
-    for it in pool.items:
-        it["out"].copy_(it["in"])
-        t0 = time.perf_counter()
-        check(L.origami_sort(it["kind"], it["out"].data_ptr(), None, it["n"], 0, 0, 0, ctypes.byref(res)))
-        dt += time.perf_counter() - t0
-    out["loop_plain_keys_per_s"] = pool.keys / dt
+    for _ in range(2):
+        for it in pool.items:
+            it["out"].copy_(it["in"])
+            t0 = time.perf_counter()
+            check(L.origami_sort(it["kind"], it["out"].data_ptr(), None, it["n"], 0, 0, 0, ctypes.byref(res)))
+            dt += time.perf_counter() - t0
+    out["loop_plain_keys_per_s"] = 2 * pool.keys / dt
     if out.get("saturation", {}).get("keys_per_s"):
         out["saturation_vs_loop_plain"] = out["saturation"]["keys_per_s"] / out["loop_plain_keys_per_s"]
     # the host link: what the largest request's copies cost at the least
