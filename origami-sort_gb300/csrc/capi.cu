@@ -415,6 +415,7 @@ uint64_t typed_scratch_io(int kind, uint64_t n, uint64_t sort_n, int fan, uint64
 // first copy starts with six, 7.40 with four, 7.51 with three, 7.97 with two,
 // 7.28 with eight.
 constexpr int HOST_LANES = 7;
+static_assert(HOST_LANES - 1 >= 4, "the first chunk's four pieces sort on four lanes");
 cudaStream_t aux_stream(int which) {
     thread_local cudaStream_t s[HOST_LANES] = {};
     if (!s[which]) cudaStreamCreateWithFlags(&s[which], cudaStreamNonBlocking);
@@ -502,6 +503,9 @@ struct HostPipePlan {
     bool slice_copies = false;
     uint64_t chunk_n = 0;
     int fan = 0, cfan = 0, mfan = 0;
+    // pinned input: the first chunk is copied in this many pieces, each sorted
+    // as it lands, then merged into the chunk's run by one k-way pass
+    int first_pieces = 1;
     uint64_t data = 0, ws = 0, wm = 0, total = 0;  // A and B (data each), lane scratch, merge scratch
 };
 
@@ -534,7 +538,13 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
     // kernel and 14.27 with 8-way passes); min_k = 2 keeps binary passes of the
     // interleaving shape, larger min_k that fan-in
     p.cfan = min_k > 2 ? shape_code(fan_of(min_k), 0) : (min_k == 2 ? shape_code(2, 2) : shape_code(16, 0));
-    p.ws = a256(typed_scratch_io(kind, p.chunk_n, 0, p.cfan, 0));
+    // the GPU would wait for a whole first chunk before any sorting starts:
+    // copied in four pieces it starts after a quarter (1 GiB u32 call from
+    // pinned memory 13.33-13.40 -> 13.25-13.28 ms); needs chunk passes of
+    // fan-in 4 or more, so that the pieces merge in one pass
+    p.first_pieces = shape_fan(p.cfan) >= 4 ? 4 : 1;
+    p.ws = a256(std::max(typed_scratch_io(kind, p.chunk_n, 0, p.cfan, 0),
+                         typed_scratch_io(kind, p.chunk_n, 0, p.cfan, p.chunk_n / p.first_pieces)));
     // the merges across chunks are one k-way pass: bound by the host link it
     // writes (1 GiB in ~5.6 ms), which hides its cost per level
     const uint64_t need = (limit + p.chunk_n - 1) / p.chunk_n;
@@ -596,6 +606,26 @@ int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void
             const int lane = (int)(c % (HOST_LANES - 1));
             cudaStream_t cst = lanes[lane];
             const void* src = static_cast<const char*>(vin) + off * ib;
+            if (c == 0 && copy_in && p.first_pieces > 1) {
+                // piece q lands in A, is sorted into B on lane q; one pass of
+                // fan-in first_pieces then merges B's runs into the chunk's run in A
+                const int np = p.first_pieces;
+                const uint64_t pn = chunk_n / np;
+                for (int q = 0; q < np && e == cudaSuccess; ++q) {
+                    char* pa = a + q * pn * ib;
+                    char* pb = b + q * pn * ib;
+                    e = cudaMemcpyAsync(pa, static_cast<const char*>(host_in) + q * pn * ib, pn * ib,
+                                        cudaMemcpyHostToDevice, sc);
+                    cudaStreamWaitEvent(lanes[q], event_on(sc), 0);
+                    if (e == cudaSuccess) e = typed_io(kind, pa, pb, pa, pb, pn, 0, m, 0, 0, p.cfan, w[q], lanes[q]);
+                    if (e == cudaSuccess) e = watch.watch(w[q] + typed_scratch_io(kind, pn, 0, p.cfan, 0) - 256, lanes[q]);
+                }
+                for (int q = 1; q < np; ++q) cudaStreamWaitEvent(lanes[0], event_on(lanes[q]), 0);
+                if (e == cudaSuccess) e = typed_io(kind, b, a, a, b, chunk_n, 0, 0, 0, pn, p.cfan, w[0], lanes[0]);
+                if (e == cudaSuccess)
+                    e = watch.watch(w[0] + typed_scratch_io(kind, chunk_n, 0, p.cfan, pn) - 256, lanes[0]);
+                continue;
+            }
             if (copy_in) {
                 e = cudaMemcpyAsync(a + off * ib, static_cast<const char*>(host_in) + off * ib, cn * ib,
                                     cudaMemcpyHostToDevice, sc);

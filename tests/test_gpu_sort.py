@@ -198,6 +198,21 @@ def test_host_chunked_pipeline(kind, n, pinned, sort_n):
     assert np.array_equal(d, expected(a, sort_n))
 
 
+@pytest.mark.parametrize("kind,n", [(og.U32, (1 << 25) + 99), (og.KV64, (1 << 24) + 3)])
+@pytest.mark.parametrize("min_k", [2, 4, 8])
+def test_host_chunked_pipeline_fan(kind, n, min_k):
+    """Pinned host sorts whose chunks use binary passes (min_k = 2: the first
+    chunk arrives whole) or k-way passes (min_k = 4, 8: the first chunk
+    arrives in four pieces, merged by one pass)."""
+    a = make(kind, n, "uniform", seed=13)
+    d = og.empty_host(kind, n, pinned=True)
+    d[:] = a
+    t = og.empty_host(kind, n, pinned=True)
+    r = og.sort(d, t, min_k=min_k)
+    assert r is d
+    assert np.array_equal(d, expected(a))
+
+
 def _golden_cases(variant):
     with open(GOLDEN) as f:
         doc = json.load(f)
