@@ -437,8 +437,9 @@ bool is_pinned(const void* p) {
 //    writes the host output, with the passes in between in two arena buffers.
 //  * Large sorts: the input is cut into chunks of chunk_n (a power of two of
 //    at least 2^22 items; 4 to 16 chunks, more than 8 above 2^26 items). Each
-//    chunk arrives in HBM (a copy-engine transfer for pinned memory, else the
-//    first kernel's own reads) and is sorted on one of six compute streams
+//    chunk lands in HBM (a copy-engine transfer for pinned memory, a copy
+//    kernel for pageable memory; device input stays where it is; the first
+//    chunk in four pieces) and is sorted on one of six compute streams
 //    while the next chunks are in flight; one k-way pass across the chunks
 //    follows and writes the host output itself, or (the serving loop, pinned
 //    output) is cut into output slices that go to the host by copies while
@@ -491,6 +492,57 @@ struct SliceCopy {
     }
 };
 
+// Moves `bytes` from host memory the device reads through the host's page
+// tables (pageable memory on Grace) into HBM: 16-byte loads, four in flight
+// per thread, grid-stride; the last bytes % 16 by the first threads. One CTA
+// of 256 threads per SM keeps the host link busy (211 GB/s with mapped pinned
+// memory from 152 CTAs on, the copy engines' rate) and leaves the SMs' other
+// slots to the chunk sorts.
+}  // namespace
+
+namespace origami {
+__global__ void __launch_bounds__(256) link_copy_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                                        uint64_t nvec, const unsigned char* __restrict__ tsrc,
+                                                        unsigned char* __restrict__ tdst, unsigned tail) {
+    constexpr int U = 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * U;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x * U + threadIdx.x; i < nvec; i += stride) {
+        uint4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t j = i + (uint64_t)u * blockDim.x;
+            if (j < nvec) v[u] = src[j];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t j = i + (uint64_t)u * blockDim.x;
+            if (j < nvec) dst[j] = v[u];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < tail) tdst[threadIdx.x] = tsrc[threadIdx.x];
+}
+}  // namespace origami
+
+namespace {
+using origami::link_copy_kernel;
+
+cudaError_t link_copy(const void* src, void* dst, uint64_t bytes, cudaStream_t st) {
+    static const unsigned grid = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return (unsigned)(sms > 0 ? sms : 1);
+    }();
+    const uint64_t nvec = bytes / 16;
+    const unsigned tail = (unsigned)(bytes % 16);
+    launch("link_copy", st, [&] {
+        link_copy_kernel<<<grid, 256, 0, st>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), nvec,
+                                                static_cast<const unsigned char*>(src) + nvec * 16,
+                                                static_cast<unsigned char*>(dst) + nvec * 16, tail);
+    });
+    return cudaGetLastError();
+}
+
 // The host pipeline's plan: whether it runs chunked, the pass shapes, and the
 // device memory it takes from one block (each part 256-byte aligned).
 struct HostPipePlan {
@@ -503,8 +555,8 @@ struct HostPipePlan {
     bool slice_copies = false;
     uint64_t chunk_n = 0;
     int fan = 0, cfan = 0, mfan = 0;
-    // pinned input: the first chunk is copied in this many pieces, each sorted
-    // as it lands, then merged into the chunk's run by one k-way pass
+    // host input: the first chunk lands in this many pieces, each sorted as
+    // it lands, then merged into the chunk's run by one k-way pass
     int first_pieces = 1;
     uint64_t data = 0, ws = 0, wm = 0, total = 0;  // A and B (data each), lane scratch, merge scratch
 };
@@ -558,10 +610,10 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
 // Sorts n items from `host_in` into `host_out` (host memory the device can
 // address through vin / vout, or device memory) with the memory of one block
 // of plan.total bytes, on `st` and this thread's helper streams; returns when
-// the result is in place. Large sorts are cut into chunks: each chunk arrives
-// in HBM (a copy-engine transfer for pinned memory, else the first kernel's
-// own reads) and is sorted on one of six streams while the next chunks are in
-// flight; the merge across chunks follows as one k-way pass that writes the
+// the result is in place. Large sorts are cut into chunks: each chunk lands
+// in HBM (a copy-engine transfer for pinned memory, a copy kernel for
+// pageable memory) and is sorted on one of six streams while the next chunks
+// are in flight; the merge across chunks follows as one k-way pass that writes the
 // host output (or, with plan.slice_copies and pinned output, is cut into
 // output slices copied to the host while the next slices merge). Small sorts
 // run one pipeline whose first kernel reads the input and whose last pass
@@ -587,10 +639,23 @@ int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void
         char* w[HOST_LANES - 1];
         for (int i = 0; i < HOST_LANES - 1; ++i) w[i] = b + p.data + (uint64_t)i * p.ws;
         char* wm = b + p.data + (HOST_LANES - 1) * p.ws;
-        const bool copy_in = is_pinned(host_in);
+        // host chunks land in HBM before they sort: pinned memory by the copy
+        // engines, pageable memory by link_copy_kernel. A chunk sort whose
+        // first kernel read the host link itself held its SMs for the
+        // transfer (1 GiB u32 from pageable memory: 16.3 ms per call). Device
+        // input (a serving request) is sorted where it is.
+        const bool pinned_in = is_pinned(host_in);
+        const bool device_in = !pinned_in && is_device_pointer(host_in);
+        const int np = device_in ? 1 : p.first_pieces;
         cudaStream_t lanes[HOST_LANES - 1] = {st};
         for (int i = 1; i < HOST_LANES - 1; ++i) lanes[i] = aux_stream(i - 1);
         cudaStream_t sc = aux_stream(HOST_LANES - 1);
+        auto land = [&](char* dst, uint64_t off_items, uint64_t items) -> cudaError_t {
+            if (pinned_in)
+                return cudaMemcpyAsync(dst, static_cast<const char*>(host_in) + off_items * ib, items * ib,
+                                       cudaMemcpyHostToDevice, sc);
+            return link_copy(static_cast<const char*>(vin) + off_items * ib, dst, items * ib, sc);
+        };
         auto event_on = [&](cudaStream_t s) {
             cudaEvent_t ev;
             cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -606,16 +671,14 @@ int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void
             const int lane = (int)(c % (HOST_LANES - 1));
             cudaStream_t cst = lanes[lane];
             const void* src = static_cast<const char*>(vin) + off * ib;
-            if (c == 0 && copy_in && p.first_pieces > 1) {
+            if (c == 0 && np > 1) {
                 // piece q lands in A, is sorted into B on lane q; one pass of
-                // fan-in first_pieces then merges B's runs into the chunk's run in A
-                const int np = p.first_pieces;
+                // fan-in np then merges B's runs into the chunk's run in A
                 const uint64_t pn = chunk_n / np;
                 for (int q = 0; q < np && e == cudaSuccess; ++q) {
                     char* pa = a + q * pn * ib;
                     char* pb = b + q * pn * ib;
-                    e = cudaMemcpyAsync(pa, static_cast<const char*>(host_in) + q * pn * ib, pn * ib,
-                                        cudaMemcpyHostToDevice, sc);
+                    e = land(pa, q * pn, pn);
                     cudaStreamWaitEvent(lanes[q], event_on(sc), 0);
                     if (e == cudaSuccess) e = typed_io(kind, pa, pb, pa, pb, pn, 0, m, 0, 0, p.cfan, w[q], lanes[q]);
                     if (e == cudaSuccess) e = watch.watch(w[q] + typed_scratch_io(kind, pn, 0, p.cfan, 0) - 256, lanes[q]);
@@ -626,9 +689,8 @@ int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void
                     e = watch.watch(w[0] + typed_scratch_io(kind, chunk_n, 0, p.cfan, pn) - 256, lanes[0]);
                 continue;
             }
-            if (copy_in) {
-                e = cudaMemcpyAsync(a + off * ib, static_cast<const char*>(host_in) + off * ib, cn * ib,
-                                    cudaMemcpyHostToDevice, sc);
+            if (!device_in) {
+                e = land(a + off * ib, off, cn);
                 cudaStreamWaitEvent(cst, event_on(sc), 0);
                 src = a + off * ib;
             }
