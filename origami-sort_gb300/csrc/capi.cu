@@ -569,12 +569,13 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
     p.fan = shape_for(kind, n, min_k);
     p.chunk_n = 1ull << 22;
     // at most 16 chunks, so that one k-way pass of fan-in 16 merges them, and
-    // more than 8 where the chunks are larger than the smallest size. The chunk sorts are bound by the GPU's sorting throughput,
-    // not by the link: the smaller the chunks, the earlier the first one
-    // arrives and the fewer levels the chunk sorts merge before the final pass,
-    // whose levels hide under its copies to the host (1 GiB u32 from pinned
-    // memory: 16 chunks 13.74 ms per call, 8 chunks 14.09 ms; the last chunk
-    // sort ends 7.40 against 7.86 ms after the first copy starts)
+    // more than 8 where the chunks are larger than the smallest size. The
+    // chunk sorts are bound by the GPU's sorting throughput, not by the link:
+    // the smaller the chunks, the earlier the first one arrives and the fewer
+    // levels the chunk sorts merge before the final pass, whose levels hide
+    // under its writes to the host (1 GiB u32 from pinned memory: 16 chunks
+    // 13.74 ms per call, 8 chunks 14.09 ms; the last chunk sort ends 7.40
+    // against 7.86 ms after the first copy starts)
     while (p.chunk_n * 16 < n) p.chunk_n <<= 1;
     p.chunked = n >= 4 * p.chunk_n && limit > p.chunk_n;
     p.data = a256(n * item_bytes(kind));
