@@ -142,17 +142,21 @@ __device__ __forceinline__ void thread_sort(T (&v)[VT], int chunk) {
 // sorted lists in global memory, A[0 .. na) and B[0 .. nb): how many of the
 // first `diag` merged items come from A, A winning ties (every merge is stable:
 // A is always the earlier run). Used by the pass partition kernels, with a few
-// interpolation steps before the bisection. When the bracket is
-// wide (late passes: runs of millions of items), the two ends are probed
-// together and up to three probes are placed by linear interpolation of
-// g(i) = key(A[i]) - key(B[diag-1-i]), which rises with i; bisection finishes
-// the narrowed bracket. On keys spread roughly evenly over their range
-// (uniform keys) the three probes leave a bracket of a few items, so the
-// chain of dependent global loads, which is the partition's whole latency,
-// shrinks from log2(run) to about ten; on any other distribution the cost is
-// at most four extra probes. The split is the first i with g(i) > 0 (A[i] >
-// B[diag-1-i]: equal keys go to A first); every decision is an exact integer
-// compare, g (in float) only places probes.
+// interpolation steps before the bisection. When the bracket is wide (late
+// passes: runs of millions of items), the two ends are probed together, then
+// up to three steps each place a probe x by linear interpolation of
+// g(i) = key(A[i]) - key(B[diag-1-i]), which rises with i, and two guard
+// probes at x -+ d, d about twice the square root of the bracket (the spread
+// of the interpolation's error on evenly spread keys). The three probes of a
+// step are independent loads, one latency; the split lands between two of
+// them, so both ends of the bracket move (a single probe moves only one, and
+// the far end stays where it was). Bisection finishes the narrowed bracket.
+// The chain of dependent global loads is the partition's whole latency: on
+// uniform keys it falls from log2(run) to about eight, and on any other
+// distribution the steps cost at most three latencies before a bisection of
+// what is left. The split is the first i with g(i) > 0 (A[i] > B[diag-1-i]:
+// equal keys go to A first); every decision is an exact integer compare, g
+// (in float) only places probes.
 // `interp` off: plain bisection (data that fits in L2, where each bisection
 // step is a short L2 hit and the interpolation arithmetic does not pay).
 template <class T>
@@ -170,16 +174,36 @@ __device__ __forceinline__ int64_t global_merge_path_interp(const T* A, int64_t 
         float gl = (float)al - (float)bl, gr = (float)ar - (float)br;
 #pragma unroll 1
         for (int step = 0; step < 3 && xr - xl > 64 && gr > gl; ++step) {
+            const int64_t span = xr - xl;
             const float f = -gl / (gr - gl);
-            int64_t x = xl + 1 + (int64_t)(f * (float)(xr - xl - 1));
+            int64_t x = xl + 1 + (int64_t)(f * (float)(span - 1));
             x = x < xl + 1 ? xl + 1 : (x > xr - 1 ? xr - 1 : x);
-            const auto a = Traits<T>::key(A[x]), b = Traits<T>::key(B[diag - 1 - x]);
-            if (a > b) {
+            int64_t d = (int64_t)(2.0f * sqrtf((float)span));
+            d = d < 16 ? 16 : d;
+            // xl < x0 <= x <= x2 < xr: every probe inside both lists
+            const int64_t x0 = x - d > xl + 1 ? x - d : xl + 1;
+            const int64_t x2 = x + d < xr - 1 ? x + d : xr - 1;
+            const auto a0 = Traits<T>::key(A[x0]), b0 = Traits<T>::key(B[diag - 1 - x0]);
+            const auto a1 = Traits<T>::key(A[x]), b1 = Traits<T>::key(B[diag - 1 - x]);
+            const auto a2 = Traits<T>::key(A[x2]), b2 = Traits<T>::key(B[diag - 1 - x2]);
+            // g rises with i: the first probe with g > 0 closes the bracket
+            // on the right, the one before it on the left
+            if (a0 > b0) {
+                xr = x0;
+                gr = (float)a0 - (float)b0;
+            } else if (a1 > b1) {
+                xl = x0;
+                gl = (float)a0 - (float)b0;
                 xr = x;
-                gr = (float)a - (float)b;
-            } else {
+                gr = (float)a1 - (float)b1;
+            } else if (a2 > b2) {
                 xl = x;
-                gl = (float)a - (float)b;
+                gl = (float)a1 - (float)b1;
+                xr = x2;
+                gr = (float)a2 - (float)b2;
+            } else {
+                xl = x2;
+                gl = (float)a2 - (float)b2;
             }
         }
         lo = xl + 1;
