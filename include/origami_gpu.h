@@ -65,9 +65,13 @@ unsigned origami_item_bytes(int kind);
  * Plain sort: the drop-in for origami_sorter::sort_single_thread
  * (reference sorter.h:3851-3915) and sort_multi_thread (sorter.h:4194-4287).
  *
- *   d, tmp   two buffers of n items each. Host pointers (pageable or pinned) are
- *            staged through the library's device arena and the result is copied
- *            back; device pointers are sorted in place with no copies.
+ *   d, tmp   two buffers of n items each. Host pointers (pageable or pinned)
+ *            that the GPU can address (pinned memory; pageable memory on hosts
+ *            whose GPU reads the host's page tables, such as Grace) are
+ *            streamed: a large sort arrives in chunks that sort while the next
+ *            ones land, and its last pass writes the result into the host
+ *            buffer. Other host pointers are staged through the library's
+ *            device arena. Device pointers are sorted in place with no copies.
  *            tmp may be NULL: device scratch is then taken from the arena.
  *   n        item count (any n >= 0)
  *   sort_n   chunk size: the array is sorted in independent chunks of sort_n
