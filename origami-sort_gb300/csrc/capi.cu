@@ -492,15 +492,15 @@ struct SliceCopy {
     }
 };
 
+}  // namespace
+
+namespace origami {
 // Moves `bytes` from host memory the device reads through the host's page
 // tables (pageable memory on Grace) into HBM: 16-byte loads, four in flight
 // per thread, grid-stride; the last bytes % 16 by the first threads. One CTA
 // of 256 threads per SM keeps the host link busy (211 GB/s with mapped pinned
 // memory from 152 CTAs on, the copy engines' rate) and leaves the SMs' other
 // slots to the chunk sorts.
-}  // namespace
-
-namespace origami {
 __global__ void __launch_bounds__(256) link_copy_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
                                                         uint64_t nvec, const unsigned char* __restrict__ tsrc,
                                                         unsigned char* __restrict__ tdst, unsigned tail) {
@@ -614,11 +614,11 @@ HostPipePlan host_pipe_plan(int kind, uint64_t n, uint64_t sort_n, unsigned min_
 // the result is in place. Large sorts are cut into chunks: each chunk lands
 // in HBM (a copy-engine transfer for pinned memory, a copy kernel for
 // pageable memory) and is sorted on one of six streams while the next chunks
-// are in flight; the merge across chunks follows as one k-way pass that writes the
-// host output (or, with plan.slice_copies and pinned output, is cut into
-// output slices copied to the host while the next slices merge). Small sorts
-// run one pipeline whose first kernel reads the input and whose last pass
-// writes the output.
+// are in flight; the merge across chunks follows as one k-way pass that
+// writes the host output (or, with plan.slice_copies and pinned output, is
+// cut into output slices copied to the host while the next slices merge).
+// Small sorts run one pipeline whose first kernel reads the input and whose
+// last pass writes the output.
 int host_pipe_run(int kind, void* host_in, void* host_out, const void* vin, void* vout, uint64_t n, uint64_t sort_n,
                   const HostPipePlan& p, void* block, cudaStream_t st) {
     const uint64_t ib = item_bytes(kind);
